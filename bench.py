@@ -1,0 +1,291 @@
+"""XPBI substep throughput on GB300: particle-substeps/s.
+
+One step = one XPBI substep over every particle of the workload (all scenes
+of a batched handle in one graph replay). Default workload: the dam-breach
+scene mix at 4M particles (four 1M-particle dam-breach scenes, seeds 0-3:
+water 600k PBF + Drucker-Prager sand 400k each, 15 XPBI + 4 PBF
+iterations, dt=1e-4). Inputs are synthetic, seeded lattices.
+
+Arms:
+  --impl xpbi       libxpbi (this repo) through its C ABI
+  --impl reference  the reference's algorithm on the host cores: the CPU
+                    oracle port (the WGSL reference path needs a WebGPU
+                    adapter, which neither machine has)
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-substeps/s at equal residual, learned warm-start vs plain, 1 GB300"
+UNIT = "particle-substeps/s"
+
+# Algorithmic bytes per particle for one launch of each kernel (compulsory
+# traffic, minimal layout): solveA reads pos 16, vel 16, F 36, L 36, state 4,
+# lambda 4 and writes lambda 4, Sp 48; solveB reads pos 16, vel 16, Sp 48 and
+# writes vel 16; pbfA reads pos 16, vel 16 and writes the PBF multiplier 4;
+# pbfB reads pos 16, vel 16, multiplier 4 and writes vel 16; computeL reads
+# pos 16, vel 16 and writes L 36; xsph reads pos, vel and writes vel 48;
+# updateF+integrate reads pos 16, vel 16, F 36, L 36, state 4 and writes pos,
+# vel, F, state 72 (148 + 64 minus the shared pos/vel reads).
+ALGO_BYTES = {"solveA": 164, "solveB": 96, "pbfA": 36, "pbfB": 52, "computeL": 68, "xsph": 48,
+              "updateF+integrate": 180, "reorder": 148, "count": 20, "fill": 8, "scan": 8}
+
+
+def workload(name: str, rank: int = 0):
+    xp = importlib.import_module("xpbi-webgpu_gb300")
+    if name == "dam_mix4":
+        scenes = xp.scenes.config_dam_mix(seeds=tuple(4 * rank + k for k in range(4)))
+    elif name == "dam_breach":
+        scenes = [xp.scenes.config_dam_breach(seed=rank)]
+    elif name == "nacc_snowball":
+        scenes = [xp.scenes.config_nacc_snowball(seed=rank)]
+    elif name == "sand_column":
+        scenes = [xp.scenes.config_sand_column(seed=rank)]
+    elif name == "batch256":
+        scenes = xp.scenes.config_batch(seed=rank)
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return xp, scenes
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        out, _ = self.p.communicate(timeout=10)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(sample_scale: float, threads: int, substeps: int = 1):
+    """The oracle port on the host cores over a bounded sample of the
+    workload: one dam-breach scene with its z extent scaled by sample_scale."""
+    from oracle import oracle as O
+    xp = importlib.import_module("xpbi-webgpu_gb300")
+    sc = xp.scenes.config_dam_breach(seed=0, scale=sample_scale)
+    pw, mw = xp.pack_uniforms(sc, xp.params_for(sc))
+    st = O.initial_state(sc)
+    n = len(sc["positions"])
+    t0 = time.perf_counter()
+    O.substep(pw, mw, st, sc["iterations"], True, sc["pbfIterations"], substeps=substeps, threads=threads)
+    dt = time.perf_counter() - t0
+    return n * substeps / dt, n, dt
+
+
+def host_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    threads = host_threads()
+    scale = args.cpu_scale
+    # warm-up + timed steps, each one substep of the bounded sample
+    for _ in range(args.warmup):
+        cpu_baseline(scale, threads)
+    times, n = [], 0
+    for _ in range(args.steps):
+        v, n, dt = cpu_baseline(scale, threads)
+        times.append(dt)
+    total = sum(times)
+    value = n * args.steps / total
+    sample = (f"dam-breach scene scaled to {n} particles (z extent x{scale}), one substep "
+              f"(15 XPBI + 4 PBF iterations) per step, f32 oracle port, {threads} threads")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": args.workload, "solver": "plain", "cpu_sample_particles": n},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_xpbi(args, rank: int, world: int):
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    xp, scenes = workload(args.workload, rank)
+    n_total = sum(len(s["positions"]) for s in scenes)
+    stream = torch.cuda.Stream()
+    sim = xp.Simulation(scenes if len(scenes) > 1 else scenes[0])
+    sim.set_stream(stream.cuda_stream)
+    has_water = any(s["hasWater"] for s in scenes)
+    for k, s in enumerate(scenes):
+        sim.write_params(xp.params_for(s), scene=k)
+        sim.set_schedule(k, s["iterations"], s["hasWater"])
+    launches = sim.launches_per_substep(-1, has_water)
+
+    # warm-up (graph capture happens here)
+    sim.step(args.warmup, -1, has_water)
+    sim.synchronize()
+
+    # ---- device-resident throughput: K graph replays, events on the launching stream
+    clocks = Clocks(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    sim.step(args.steps, -1, has_water)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    sim.synchronize()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = n_total * world * args.steps / (ms / 1e3)
+
+    # ---- end to end through the public API with host buffers: per step the
+    # frame's writeParams from host memory, one substep, and the positions
+    # read back into pinned host memory
+    pinned = [torch.empty((len(s["positions"]), 4), dtype=torch.float32, pin_memory=True).numpy()
+              for s in scenes]
+    params = [xp.params_for(s) for s in scenes]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for k in range(len(scenes)):
+            sim.write_params(params[k], scene=k)
+        sim.step(1, -1, has_water)
+        for k in range(len(scenes)):
+            sim.read_pos(k, out=pinned[k])
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = n_total * world * args.steps / e2e_s
+    # uniforms uploaded per step: SceneDev (192 B) + MatDev table (8 x 48 B)
+    # + packed material words (8 x 64 B) per scene
+    h2d = len(scenes) * (192 + 8 * 48 + 8 * 64)
+    d2h = 16 * n_total
+
+    # ---- per-kernel times (events around each launch) for the roofline
+    per = {}
+    for _ in range(max(1, args.profile_substeps)):
+        prof = sim.profile_substep(-1, has_water)
+        for line in prof.splitlines():
+            if ":" not in line:
+                continue
+            name, t = line.rsplit(":", 1)
+            per.setdefault(name.strip(), []).append(float(t.strip().replace("ms", "")))
+    total_ms = sum(sum(v) for v in per.values())
+    dom = max(per, key=lambda k: sum(per[k]))
+    dom_avg_ms = statistics.mean(per[dom])
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+        peak_src = "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    achieved = ALGO_BYTES.get(dom, 0) * n_total / (dom_avg_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
+                "algo_bytes_per_particle": ALGO_BYTES.get(dom),
+                "share": sum(per[dom]) / total_ms,
+                "kernel_ms": {k: round(statistics.mean(v), 4) for k, v in per.items()}}
+    sim.close()
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": args.workload, "particles_per_gpu": n_total, "scenes": len(scenes),
+                      "solver": "plain", "iterations": [s["iterations"] for s in scenes][:4],
+                      "l2": "inputs larger than L2 (state ~1.3 GB per 4M particles)"},
+           "roofline": roofline, "clocks": clk, "gpu_launches": launches * args.steps,
+           "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}}
+    if rank == 0 and not args.no_cpu_baseline:
+        v, n, dt = cpu_baseline(args.cpu_scale, host_threads())
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": host_threads(), "kind": "port",
+                               "sample": f"f32 oracle port, one dam-breach substep (15 XPBI + 4 PBF "
+                                         f"iterations) of {n} particles, {dt:.1f} s"}
+    if rank == 0:
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="xpbi", choices=["xpbi", "reference"])
+    ap.add_argument("--workload", default="dam_mix4")
+    ap.add_argument("--cpu-scale", type=float, default=0.25)
+    ap.add_argument("--profile-substeps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_xpbi(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

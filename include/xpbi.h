@@ -1,0 +1,191 @@
+/*
+ * xpbi.h — C ABI of libxpbi, the GB300 (sm_103a) XPBI substep.
+ *
+ * The ABI mirrors the `Simulation` class of Chiplis/xpbi-webgpu
+ * (web/js/sim.js:9-273) and the frame loop that drives it
+ * (web/js/main.js:385-415). Every entry point is `extern "C"`, takes plain
+ * pointers and sizes, returns an int status (XPBI_OK == 0) and records a
+ * message retrievable with xpbi_last_error(). A handle is confined to one host
+ * thread at a time. All device work is ordered on the handle's CUDA stream.
+ *
+ * Layouts at this boundary are the reference's buffer layouts
+ * (sim.js:32-82): positions and velocities are vec4 x N (pos.w = material
+ * index + colour seed in [0, 0.49); vel.w = V^n), the deformation gradient and
+ * the kernel-gradient correction are mat3x3f x N (3 columns padded to vec4:
+ * 12 floats per particle), aux is vec4 x N (V^n, lambda, plastic state,
+ * PBF lambda), sortedIdx is u32 x N and the cell table u32 x numCells.
+ */
+#ifndef XPBI_H
+#define XPBI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  XPBI_OK = 0,
+  XPBI_ERR_INVALID = 1, /* bad argument or scene descriptor */
+  XPBI_ERR_CUDA = 2,    /* a CUDA runtime call failed */
+  XPBI_ERR_OOM = 3,     /* device allocation failed */
+  XPBI_ERR_DEVICE = 4   /* a kernel raised its error word (bounded wait expired) */
+};
+
+/* Material kinds, sim.js:4-7 (MAT). */
+enum {
+  XPBI_ELASTIC = 0,
+  XPBI_DP = 1,
+  XPBI_NACC = 2,
+  XPBI_VM = 3,
+  XPBI_HB = 4,
+  XPBI_SNOW = 5,
+  XPBI_WATER = 6
+};
+
+#define XPBI_MAX_MATERIALS 8 /* MATS : array<Material, 8>, simkernels.js:19 */
+#define XPBI_PARAMS_WORDS 64 /* 256-byte Params uniform, sim.js:160 */
+#define XPBI_MATERIAL_WORDS 16 /* MAT_STRIDE, sim.js:4 */
+
+/* One material parameter set as written by the scene factories
+ * (web/js/scenes.js:40-80) and consumed by writeMaterials (sim.js:84-99):
+ * DP (p0 = alpha, p1 = cohesion), NACC (p1 = beta, p2 = xi, p3 = M),
+ * VM (p0 = sigmaY), HB (p0 = sigmaY, p1 = h, p2 = eta),
+ * SNOW (p0 = thetaC, p1 = thetaS, p2 = xi). */
+typedef struct xpbi_material {
+  uint32_t kind;
+  double E, nu, density; /* f64 like the JS numbers they replace; */
+  double p0, p1, p2, p3; /* derived values are rounded to f32 once */
+  float color[3];
+  double bound_friction; /* scenes default 0.4 (sim.js:95) */
+} xpbi_material;
+
+/* A scene as handed to `new Simulation(device, scene)` (sim.js:10-30, 52-81).
+ * states, velocities and color_seeds may be NULL (zeros; seeds 0). */
+typedef struct xpbi_scene_desc {
+  uint32_t n;                /* particles */
+  const float* positions;    /* 3N */
+  const uint32_t* mat_ids;   /* N, each < n_materials */
+  const float* states;       /* N or NULL: initial plastic state (aux.z) */
+  const float* velocities;   /* 3N or NULL */
+  const float* color_seeds;  /* N or NULL: fraction added to pos.w, [0, 0.49) */
+  double h;                  /* particle spacing r; support = 2h (f64 as in JS) */
+  double domain_min[3];      /* grid sizing runs in f64 (sim.js:20-26) */
+  double domain_max[3];
+  uint32_t n_materials;      /* 1..8 */
+  const xpbi_material* materials;
+} xpbi_scene_desc;
+
+/* Per-frame parameters of writeParams (sim.js:159-186, main.js:392-402).
+ * pbf_iterations < 0 keeps the reference schedule (one PBF pass after every
+ * XPBI iteration); k >= 0 runs PBF after the first k iterations only. */
+typedef struct xpbi_params {
+  float dt;
+  float domain_min[3];
+  float domain_max[3];
+  float gravity[3];
+  float collider_pos[3];
+  float collider_r;
+  float collider_vel[3];
+  int32_t collider_active;
+  float xsph_c;        /* scenes.js:88 default 0.01 */
+  float omega;         /* 0.5 */
+  float contact_omega; /* 0.4 */
+  float pbf_eps;       /* 100 */
+  float s_corr_k;      /* 1e-4 */
+  float time;          /* written, never read by a kernel (sim.js:185) */
+  float k_damp;        /* 0.4 (sim.js:184) */
+  int32_t pbf_iterations;
+} xpbi_params;
+
+typedef struct xpbi_sim xpbi_sim;
+
+/* Text of the last error raised on this thread ("" if none). */
+const char* xpbi_last_error(void);
+
+/* Host-only: grid sizing (sim.js:20-26), material packing (sim.js:84-99) and
+ * Params packing (sim.js:159-186) into the reference's uniform words. No GPU
+ * needed. params may be NULL (dt and friends left 0). */
+int xpbi_pack_uniforms(const xpbi_scene_desc* scene, const xpbi_params* params,
+                       uint32_t params_words[XPBI_PARAMS_WORDS],
+                       uint32_t material_words[XPBI_MAX_MATERIALS * XPBI_MATERIAL_WORDS]);
+
+/* constructor + createBuffers + createPipelines (sim.js:10-30, 32-82, 101-156).
+ * Allocates all device buffers on the current CUDA device. */
+int xpbi_create(const xpbi_scene_desc* scene, xpbi_sim** out);
+
+/* Batched form: many independent scenes (uneven sizes, mixed materials) in one
+ * handle; every stage runs as one launch over all scenes. Not in the
+ * reference (one scene per Simulation). */
+int xpbi_batch_create(const xpbi_scene_desc* scenes, uint32_t n_scenes, xpbi_sim** out);
+
+void xpbi_destroy(xpbi_sim* sim);
+
+/* writeMaterials (sim.js:84-99); scene < 0 applies to every scene. */
+int xpbi_write_materials(xpbi_sim* sim, int32_t scene, const xpbi_material* materials, uint32_t n);
+
+/* writeParams (sim.js:159-186); scene < 0 applies to every scene. */
+int xpbi_write_params(xpbi_sim* sim, int32_t scene, const xpbi_params* params);
+
+/* Per-scene solver schedule for batched handles (each scene of a batch may
+ * use its own iteration count and water flag). */
+int xpbi_set_schedule(xpbi_sim* sim, int32_t scene, int32_t iterations, int32_t has_water);
+
+/* encodeSubstep (sim.js:220-272): enqueue one substep for every scene with
+ * the given iteration count and water flag (iterations < 0: per-scene
+ * schedule from xpbi_set_schedule). Asynchronous. */
+int xpbi_encode_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water);
+
+/* The frame loop's substep loop (main.js:406-413): `substeps` substeps,
+ * replayed from a captured CUDA graph of one substep. Asynchronous. */
+int xpbi_step(xpbi_sim* sim, int32_t substeps, int32_t iterations, int32_t has_water);
+
+/* Wait for the handle's stream and report device-side errors. */
+int xpbi_synchronize(xpbi_sim* sim);
+
+/* Run subsequent work on a caller's cudaStream_t (NULL: the handle's own). */
+int xpbi_set_stream(xpbi_sim* sim, void* cuda_stream);
+
+/* __XPBI.readPos / readVel (main.js:291-312): vec4 x N of scene `scene`
+ * (0 for single-scene handles), in the current (cell-sorted) order. */
+int xpbi_read_positions(xpbi_sim* sim, uint32_t scene, float* out_pos4);
+int xpbi_read_velocities(xpbi_sim* sim, uint32_t scene, float* out_vel4);
+
+/* Full state of one scene in the reference layouts; any pointer may be NULL.
+ * cell_tab receives the scene's numCells cell start offsets after the last
+ * substep's scatter (simkernels.js:131-147), sorted_idx its permutation. */
+int xpbi_read_state(xpbi_sim* sim, uint32_t scene, float* pos4, float* vel4, float* F12, float* L12,
+                    float* aux4, uint32_t* sorted_idx, uint32_t* cell_tab);
+
+/* Overwrite one scene's state (pos4, vel4, F12, aux4; NULL keeps a field). */
+int xpbi_write_state(xpbi_sim* sim, uint32_t scene, const float* pos4, const float* vel4, const float* F12,
+                     const float* aux4);
+
+/* The uniform words the kernels of scene `scene` consume (as packed by
+ * xpbi_pack_uniforms after the last write_params / write_materials). */
+int xpbi_read_uniforms(xpbi_sim* sim, uint32_t scene, uint32_t params_words[XPBI_PARAMS_WORDS],
+                       uint32_t material_words[XPBI_MAX_MATERIALS * XPBI_MATERIAL_WORDS]);
+
+/* Sizes: total particles, total cells, scenes; dims of scene 0 (may be NULL). */
+int xpbi_info(xpbi_sim* sim, uint32_t* n_particles, uint32_t* n_cells, uint32_t* n_scenes, int32_t dims[3]);
+
+/* profileSubstep (sim.js:199-215): runs one substep with a CUDA event around
+ * every launch; ms[k] is launch k's time, labels (may be NULL) receives
+ * "label: x.xxxms" lines. *count = number of launches recorded. */
+int xpbi_profile_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water, float* ms, int32_t cap,
+                         int32_t* count, char* labels, size_t labels_cap);
+
+/* Borrowed device pointers for a renderer (posBuf, velA, matsBuf bound in
+ * main.js:189-199): float4 positions, float4 velocities (both cell-sorted,
+ * all scenes concatenated) and the packed material table. */
+int xpbi_device_ptrs(xpbi_sim* sim, void** pos4, void** vel4, void** materials);
+
+/* Number of kernel launches one substep issues with this schedule. */
+int xpbi_launches_per_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XPBI_H */

@@ -1,0 +1,140 @@
+"""GPU parity: libxpbi's substep vs the CPU oracle from identical state.
+
+Every case calls the C ABI through the package's ctypes binding, runs the
+same substep in the oracle, and checks the sort bit-exactly and the FP32
+particle state within 1e-4 normwise relative error (parity_util.REL_TOL).
+"""
+import numpy as np
+import pytest
+
+from parity_util import REL_TOL, compare, rel, run_pair
+
+pytestmark = pytest.mark.gpu
+
+
+def _scene(xp, name, **kw):
+    return getattr(xp.scenes, name)(**kw)
+
+
+@pytest.mark.parametrize("warm", [0, 5])
+def test_sand_column_config(xp, oracle, built_lib, warm):
+    sc = xp.scenes.config_sand_column()
+    s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=warm)
+    rep = compare(s1, ref, ref64)
+    print("sand_column", warm, rep)
+
+
+def test_sand_column_after_collapse_starts(xp, oracle, built_lib):
+    sc = xp.scenes.config_sand_column()
+    s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=60)
+    # by now the column is flowing: multipliers and plastic projection active
+    assert np.abs(ref["aux"][:, 1]).max() > 0
+    compare(s1, ref, ref64)
+
+
+@pytest.mark.parametrize("name", ["sand_column", "sand_two_blocks", "snowball_smash", "plasticine",
+                                  "goo", "snow_classic", "dam_breach", "elastic_block"])
+def test_reference_demo_scenes(xp, oracle, built_lib, name):
+    sc = _scene(xp, name)
+    s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=12)
+    rep = compare(s1, ref, ref64, has_pbf=sc["hasWater"])
+    print(name, len(sc["positions"]), rep)
+
+
+def test_nacc_snowball_wall_impact(xp, oracle, built_lib):
+    sc = xp.scenes.config_nacc_snowball()
+    # ~120 substeps until the sphere reaches the wall; start near impact
+    s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=125)
+    compare(s1, ref, ref64)
+
+
+def test_dam_breach_small(xp, oracle, built_lib):
+    sc = xp.scenes.config_dam_breach(scale=0.05)
+    s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=10)
+    compare(s1, ref, ref64, has_pbf=True)
+
+
+def test_reference_pbf_interleave(xp, oracle, built_lib):
+    """pbfIterations unset: one PBF pass after every XPBI iteration."""
+    sc = xp.scenes.config_dam_breach(scale=0.05)
+    p = xp.params_for(sc, pbfIterations=None)
+    s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=3, params=p)
+    compare(s1, ref, ref64, has_pbf=True)
+
+
+def test_collider_active(xp, oracle, built_lib):
+    sc = xp.scenes.plasticine()
+    p = xp.params_for(sc, colliderActive=True, colliderPos=[0.5, 0.45, 0.5], colliderR=0.08,
+                      colliderVel=[0.3, -0.5, 0.0])
+    s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=4, params=p)
+    compare(s1, ref, ref64)
+
+
+def test_zero_iterations(xp, oracle, built_lib):
+    sc = xp.scenes.elastic_block()
+    s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=2, iterations=0)
+    compare(s1, ref, ref64)
+
+
+def test_graph_step_matches_encode(xp, built_lib):
+    """xpbi_step (graph replay) and xpbi_encode_substep give identical bytes."""
+    sc = xp.scenes.snow_classic()
+    p = xp.params_for(sc)
+    out = []
+    for use_graph in (True, False):
+        with xp.Simulation(sc) as sim:
+            sim.write_params(p)
+            if use_graph:
+                sim.step(7, sc["iterations"], False)
+            else:
+                for _ in range(7):
+                    sim.encode_substep(sc["iterations"], False)
+            out.append(sim.read_state())
+    for k in ("pos", "vel", "F", "aux", "sortedIdx", "cellTab"):
+        assert np.array_equal(out[0][k], out[1][k]), k
+
+
+def test_deterministic_rerun(xp, built_lib):
+    sc = xp.scenes.dam_breach()
+    p = xp.params_for(sc)
+    out = []
+    for _ in range(2):
+        with xp.Simulation(sc) as sim:
+            sim.write_params(p)
+            sim.step(10, sc["iterations"], True)
+            out.append(sim.read_state())
+    for k in ("pos", "vel", "F", "L", "aux", "sortedIdx", "cellTab"):
+        assert np.array_equal(out[0][k], out[1][k]), k
+
+
+def test_batched_scenes_match_single(xp, oracle, built_lib):
+    """A batch of uneven scenes with mixed materials: every scene's substep
+    matches its own oracle run (sort bit-exact, state within tolerance)."""
+    scenes = [xp.scenes.plasticine(), xp.scenes.snowball_smash(), xp.scenes.goo(), xp.scenes.dam_breach(),
+              xp.scenes.snow_classic()]
+    iters = [4, 3, 5, 2, 6]
+    with xp.Simulation(scenes) as sim:
+        for k, sc in enumerate(scenes):
+            sim.write_params(xp.params_for(sc), scene=k)
+            sim.set_schedule(k, iters[k], sc["hasWater"])
+        sim.step(3, -1, False)
+        states = [sim.read_state(k) for k in range(len(scenes))]
+        uni = [sim.uniforms(k) for k in range(len(scenes))]
+        sim.encode_substep(-1, False)
+        after = [sim.read_state(k) for k in range(len(scenes))]
+    for k, sc in enumerate(scenes):
+        pw, mw = uni[k]
+        ref = oracle.substep(pw, mw, states[k], iters[k], sc["hasWater"], -1)
+        compare(after[k], ref, has_pbf=sc["hasWater"])
+
+
+def test_profile_substep_labels(xp, built_lib):
+    sc = xp.scenes.dam_breach()
+    with xp.Simulation(sc) as sim:
+        sim.write_params(xp.params_for(sc))
+        text = sim.profile_substep(3, True)
+        n = sim.launches_per_substep(3, True)
+    lines = [l for l in text.splitlines() if l]
+    assert len(lines) == n - 1  # the crowded-cell pass is timed with the reorder
+    assert lines[0].startswith("count:") and lines[-1].startswith("updateF+integrate:")
+    assert sum(1 for l in lines if l.startswith("pbfB")) == 3

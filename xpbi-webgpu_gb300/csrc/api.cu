@@ -1,0 +1,878 @@
+// C ABI of libxpbi (declared in include/xpbi.h): the GB300 counterpart of the
+// reference's `Simulation` class (web/js/sim.js:9-273) and of the frame
+// loop's substep loop (web/js/main.js:385-415).
+//
+// Host packing here follows sim.js exactly where it feeds the kernels: grid
+// sizing in f64 (sim.js:20-26), material derivation mu/lambda/mass in f64
+// (sim.js:84-99), Params words (sim.js:159-186). Constants that the WGSL
+// re-derives per call (kernel normalisations, alpha-tilde, caps) are formed
+// once per writeParams in f32 with the same operation order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "xpbi.h"
+#include "xpbi_internal.h"
+
+using namespace xpbi;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define XPBI_CK(call)                                                                      \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) {                                                               \
+      return fail(e_ == cudaErrorMemoryAllocation ? XPBI_ERR_OOM : XPBI_ERR_CUDA,          \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                     \
+    }                                                                                      \
+  } while (0)
+
+struct SceneHost {
+  uint32_t n = 0, pBase = 0, cellBase = 0, numCells = 0;
+  double h = 0, support = 0, V0 = 0;
+  double dmin[3] = {0, 0, 0}, dmax[3] = {0, 0, 0};
+  double origin[3] = {0, 0, 0};
+  int dims[3] = {0, 0, 0};
+  xpbi_material mats[kMaxMats];
+  uint32_t nMats = 0;
+  xpbi_params params;
+  int iterations = 0, hasWater = 0;
+};
+
+float f32(double x) { return (float)x; }
+uint32_t bits(float x) {
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  return u;
+}
+
+// sim.js:20-26
+int sizeGrid(const xpbi_scene_desc& d, SceneHost& s) {
+  if (!(d.h > 0) || !std::isfinite(d.h)) return fail(XPBI_ERR_INVALID, "scene h must be positive and finite");
+  s.h = d.h;
+  s.support = 2 * d.h;
+  s.V0 = std::pow(d.h, 3.0);
+  const double cs = s.support;
+  const int pad = 2;
+  double cells = 1;
+  for (int k = 0; k < 3; ++k) {
+    if (!(d.domain_max[k] > d.domain_min[k])) return fail(XPBI_ERR_INVALID, "scene domain_max must exceed domain_min");
+    s.dmin[k] = d.domain_min[k];
+    s.dmax[k] = d.domain_max[k];
+    s.origin[k] = d.domain_min[k] - pad * cs;
+    double dim = std::ceil((d.domain_max[k] - d.domain_min[k]) / cs) + 2 * pad;
+    if (!(dim >= 1) || dim > 1e6) return fail(XPBI_ERR_INVALID, "scene grid dimension out of range");
+    s.dims[k] = (int)dim;
+    cells *= dim;
+  }
+  if (cells > 2147483647.0) return fail(XPBI_ERR_INVALID, "scene grid has too many cells");
+  s.numCells = (uint32_t)cells;
+  return XPBI_OK;
+}
+
+void defaultParams(const SceneHost& s, xpbi_params& p) {
+  std::memset(&p, 0, sizeof(p));
+  p.dt = 0;
+  for (int k = 0; k < 3; ++k) {
+    p.domain_min[k] = (float)s.dmin[k];
+    p.domain_max[k] = (float)s.dmax[k];
+  }
+  p.gravity[1] = -9.8f;  // scenes.js:86
+  p.xsph_c = 0.01f;
+  p.omega = 0.5f;
+  p.contact_omega = 0.4f;
+  p.pbf_eps = 100.f;
+  p.s_corr_k = 1e-4f;
+  p.k_damp = 0.4f;
+  p.pbf_iterations = -1;
+}
+
+// sim.js:84-99 (one material into 16 words)
+void packMaterial(const xpbi_material& m, double V0, uint32_t* o) {
+  const double E = m.E, nu = m.nu;
+  const double mu = E / (2 * (1 + nu));
+  const double lam = E * nu / ((1 + nu) * (1 - 2 * nu));
+  o[0] = bits(f32(mu));
+  o[1] = bits(f32(lam));
+  o[2] = bits(f32(m.density));
+  o[3] = m.kind;
+  o[4] = bits(f32(m.p0));
+  o[5] = bits(f32(m.p1));
+  o[6] = bits(f32(m.p2));
+  o[7] = bits(f32(m.p3));
+  o[8] = bits(m.color[0]);
+  o[9] = bits(m.color[1]);
+  o[10] = bits(m.color[2]);
+  o[11] = bits(1.f);
+  o[12] = bits(f32(m.bound_friction));
+  o[13] = bits(f32(m.density * V0));
+  o[14] = 0;
+  o[15] = 0;
+}
+
+// sim.js:159-186
+void packParams(const SceneHost& s, const xpbi_params& p, uint32_t* w) {
+  std::memset(w, 0, 4 * XPBI_PARAMS_WORDS);
+  for (int k = 0; k < 3; ++k) {
+    w[k] = bits(f32(s.origin[k]));
+    w[4 + k] = (uint32_t)s.dims[k];
+    w[8 + k] = bits(p.domain_min[k]);
+    w[12 + k] = bits(p.domain_max[k]);
+    w[16 + k] = bits(p.gravity[k]);
+    w[20 + k] = bits(p.collider_pos[k]);
+    w[24 + k] = bits(p.collider_vel[k]);
+  }
+  w[3] = bits(f32(s.support));
+  w[7] = s.numCells;
+  w[11] = bits(p.dt);
+  w[15] = bits(f32(s.h));
+  w[19] = bits(f32(s.support));
+  w[23] = bits(p.collider_r);
+  w[27] = bits(p.collider_active ? 1.f : 0.f);
+  w[28] = s.n;
+  w[29] = bits(f32(s.V0));
+  w[30] = bits(p.xsph_c);
+  w[31] = bits(p.omega);
+  w[32] = bits(p.pbf_eps);
+  w[33] = bits(p.s_corr_k);
+  w[34] = bits(p.time);
+  w[35] = bits(p.contact_omega);
+  w[36] = bits(p.k_damp);
+}
+
+float wf(const uint32_t* w, int k) {
+  float x;
+  std::memcpy(&x, &w[k], 4);
+  return x;
+}
+
+// Device uniforms from the packed words. Every float here is read back from
+// the packed words, so kernels see exactly the f32 values the WGSL would.
+void buildSceneDev(const SceneHost& s, uint32_t sceneIdx, SceneDev& d, MatDev* md) {
+  uint32_t w[XPBI_PARAMS_WORDS], m[kMaxMats * XPBI_MATERIAL_WORDS];
+  packParams(s, s.params, w);
+  std::memset(m, 0, sizeof(m));
+  for (uint32_t i = 0; i < s.nMats; ++i) packMaterial(s.mats[i], s.V0, m + 16 * i);
+  std::memset(&d, 0, sizeof(d));
+  for (int k = 0; k < 3; ++k) {
+    d.origin[k] = wf(w, k);
+    d.dims[k] = (int)w[4 + k];
+    d.dmin[k] = wf(w, 8 + k);
+    d.dmax[k] = wf(w, 12 + k);
+    d.grav[k] = wf(w, 16 + k);
+    d.colPos[k] = wf(w, 20 + k);
+    d.colVel[k] = wf(w, 24 + k);
+  }
+  d.cs = wf(w, 3);
+  d.numCells = w[7];
+  d.cellBase = s.cellBase;
+  d.pBase = s.pBase;
+  d.n = s.n;
+  d.matBase = sceneIdx * kMaxMats;
+  d.dt = wf(w, 11);
+  d.h = wf(w, 15);
+  d.support = wf(w, 19);
+  d.colR = wf(w, 23);
+  d.colActive = wf(w, 27);
+  d.V0 = wf(w, 29);
+  d.xsphC = wf(w, 30);
+  d.omega = wf(w, 31);
+  d.pbfEps = wf(w, 32);
+  d.sCorrK = wf(w, 33);
+  d.contactOmega = wf(w, 35);
+  d.kDamp = wf(w, 36);
+  const float h = d.h, H = d.support, dt = d.dt;
+  d.support2 = H * H;
+  d.sigW = 21.f / ((float)(16.0 * 3.14159265) * h * h * h);
+  d.poly6C = 315.f / ((float)(64.0 * 3.14159265) * powf(H, 9.f));
+  d.spikyC = -45.f / ((float)3.14159265 * powf(H, 6.f));
+  {
+    const float x = H * H - 0.f * 0.f;
+    d.w00 = d.poly6C * x * x * x;
+  }
+  {
+    const float r = 0.2f * H;
+    if (r >= H) d.w0 = 0.f;
+    else {
+      const float x = H * H - r * r;
+      d.w0 = d.poly6C * x * x * x;
+    }
+  }
+  d.alphaT = (1.f / d.V0) / (dt * dt);
+  d.minD = 0.75f * h;
+  d.vmaxCFL = 0.45f * H / dt;
+  d.dvCap = 0.2f * H / dt;
+  d.iterations = s.iterations;
+  d.pbfIterations = s.params.pbf_iterations;
+  d.hasWater = s.hasWater;
+  for (int i = 0; i < kMaxMats; ++i) {
+    const uint32_t* q = m + 16 * i;
+    MatDev& M = md[i];
+    std::memset(&M, 0, sizeof(M));
+    M.mu = wf(q, 0);
+    M.lam = wf(q, 1);
+    M.density = wf(q, 2);
+    M.kind = q[3];
+    M.p0 = wf(q, 4);
+    M.p1 = wf(q, 5);
+    M.p2 = wf(q, 6);
+    M.p3 = wf(q, 7);
+    M.boundFriction = wf(q, 12);
+    M.mass = wf(q, 13);
+  }
+}
+
+int validateScene(const xpbi_scene_desc* d) {
+  if (!d) return fail(XPBI_ERR_INVALID, "scene descriptor is NULL");
+  if (d->n > 0 && (!d->positions || !d->mat_ids)) return fail(XPBI_ERR_INVALID, "positions and mat_ids are required");
+  if (d->n_materials < 1 || d->n_materials > (uint32_t)kMaxMats || !d->materials)
+    return fail(XPBI_ERR_INVALID, "n_materials must be 1..8 with a materials array");
+  for (uint32_t i = 0; i < d->n_materials; ++i)
+    if (d->materials[i].kind > XPBI_WATER) return fail(XPBI_ERR_INVALID, "material kind out of range");
+  for (uint32_t i = 0; i < d->n; ++i)
+    if (d->mat_ids[i] >= d->n_materials) return fail(XPBI_ERR_INVALID, "mat_ids entry >= n_materials");
+  return XPBI_OK;
+}
+
+}  // namespace
+
+struct xpbi_sim {
+  int device = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaStream_t capture = nullptr;
+  Bufs b{};
+  std::vector<SceneHost> sc;
+  std::vector<SceneDev> sdev;
+  std::vector<MatDev> mdev;
+  std::vector<uint32_t> matWordsHost;
+  uint32_t* matWords = nullptr;  // packed reference material table [S*128] (renderer binding)
+  bool dirty = true;
+  bool fresh = true;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  std::string gkey;
+  std::vector<void*> allocs;
+};
+
+namespace {
+
+template <class T>
+int alloc(xpbi_sim* s, T** p, size_t count) {
+  void* q = nullptr;
+  size_t bytes = std::max<size_t>(count * sizeof(T), 256);
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) return fail(XPBI_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  s->allocs.push_back(q);
+  *p = (T*)q;
+  return XPBI_OK;
+}
+
+#define XPBI_TRY(x)               \
+  do {                            \
+    int r_ = (x);                 \
+    if (r_ != XPBI_OK) return r_; \
+  } while (0)
+
+void destroyAll(xpbi_sim* s) {
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  if (s->graph) cudaGraphDestroy(s->graph);
+  for (void* p : s->allocs) cudaFree(p);
+  if (s->own) cudaStreamDestroy(s->own);
+  if (s->capture) cudaStreamDestroy(s->capture);
+}
+
+int upload(xpbi_sim* s) {
+  if (!s->dirty) return XPBI_OK;
+  const uint32_t S = (uint32_t)s->sc.size();
+  s->sdev.resize(S);
+  s->mdev.resize((size_t)S * kMaxMats);
+  s->matWordsHost.assign((size_t)S * kMaxMats * XPBI_MATERIAL_WORDS, 0u);
+  for (uint32_t i = 0; i < S; ++i) {
+    buildSceneDev(s->sc[i], i, s->sdev[i], &s->mdev[(size_t)i * kMaxMats]);
+    for (uint32_t m = 0; m < s->sc[i].nMats; ++m)
+      packMaterial(s->sc[i].mats[m], s->sc[i].V0, &s->matWordsHost[((size_t)i * kMaxMats + m) * XPBI_MATERIAL_WORDS]);
+  }
+  XPBI_CK(cudaMemcpyAsync(s->b.scenes, s->sdev.data(), sizeof(SceneDev) * S, cudaMemcpyHostToDevice, s->stream));
+  XPBI_CK(cudaMemcpyAsync(s->b.mats, s->mdev.data(), sizeof(MatDev) * s->mdev.size(), cudaMemcpyHostToDevice,
+                          s->stream));
+  XPBI_CK(cudaMemcpyAsync(s->matWords, s->matWordsHost.data(), 4 * s->matWordsHost.size(), cudaMemcpyHostToDevice,
+                          s->stream));
+  s->dirty = false;
+  return XPBI_OK;
+}
+
+// The substep's launch schedule: max iterations and which iterations run PBF.
+struct Schedule {
+  int K = 0;
+  std::vector<char> pbf;
+  std::string key() const {
+    std::string k = std::to_string(K) + ":";
+    for (char c : pbf) k += c ? '1' : '0';
+    return k;
+  }
+};
+
+Schedule schedule(const xpbi_sim* s) {
+  Schedule sch;
+  for (const SceneHost& h : s->sc) sch.K = std::max(sch.K, h.iterations);
+  sch.pbf.assign(sch.K, 0);
+  for (const SceneHost& h : s->sc) {
+    if (!h.hasWater) continue;
+    for (int k = 0; k < h.iterations; ++k)
+      if (h.params.pbf_iterations < 0 || k < h.params.pbf_iterations) sch.pbf[k] = 1;
+  }
+  return sch;
+}
+
+struct Recorder {
+  // optional per-launch event timing (profileSubstep)
+  std::vector<cudaEvent_t>* ev = nullptr;
+  std::vector<std::string>* labels = nullptr;
+  void mark(cudaStream_t st, const char* label) {
+    if (!ev) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, st);
+    ev->push_back(e);
+    if (label) labels->push_back(label);
+  }
+};
+
+// encodeSubstep (sim.js:220-272). Ping-pong parity is resolved on the host:
+// the last writer's buffer is passed to updateF+integrate directly, so no
+// copy-back is needed (the reference copies velB -> velA when odd).
+void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder* rec) {
+  const Bufs& b = s->b;
+  Recorder none;
+  Recorder& R = rec ? *rec : none;
+  R.mark(st, nullptr);
+  launch_count(b, st);
+  R.mark(st, "count");
+  launch_scan(b, st);
+  R.mark(st, "scan");
+  launch_scatter(b, st);
+  R.mark(st, "fill");
+  launch_reorder(b, st);
+  R.mark(st, "reorder");
+  launch_computeL(b, st);
+  R.mark(st, "computeL");
+  int in = 0;
+  for (int k = 0; k < sch.K; ++k) {
+    launch_solveA(b, k, b.velS[in], st);
+    R.mark(st, "solveA");
+    launch_solveB(b, k, b.velS[in], b.velS[in ^ 1], st);
+    R.mark(st, "solveB");
+    in ^= 1;
+    if (sch.pbf[k]) {
+      launch_pbfA(b, k, b.velS[in], st);
+      R.mark(st, "pbfA");
+      launch_pbfB(b, k, b.velS[in], b.velS[in ^ 1], st);
+      R.mark(st, "pbfB");
+      in ^= 1;
+    }
+  }
+  launch_xsph(b, b.velS[in], b.velS[in ^ 1], st);
+  R.mark(st, "xsph");
+  in ^= 1;
+  launch_updateF_integrate(b, b.velS[in], st);
+  R.mark(st, "updateF+integrate");
+}
+
+int kernelsPerSubstep(const Schedule& sch) {
+  int n = 5 /* count, scan, fill, bigcells, reorder */ + 1 /* computeL */ + 2 /* xsph, updateF+integrate */;
+  for (int k = 0; k < sch.K; ++k) n += 2 + (sch.pbf[k] ? 2 : 0);
+  return n;
+}
+
+int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) {
+  if (!out) return fail(XPBI_ERR_INVALID, "out handle pointer is NULL");
+  *out = nullptr;
+  if (nScenes < 1 || nScenes > 65535) return fail(XPBI_ERR_INVALID, "n_scenes must be 1..65535");
+  std::vector<SceneHost> sc(nScenes);
+  uint64_t N = 0, C = 0;
+  for (uint32_t i = 0; i < nScenes; ++i) {
+    XPBI_TRY(validateScene(&scenes[i]));
+    SceneHost& h = sc[i];
+    XPBI_TRY(sizeGrid(scenes[i], h));
+    h.n = scenes[i].n;
+    h.pBase = (uint32_t)N;
+    h.cellBase = (uint32_t)C;
+    h.nMats = scenes[i].n_materials;
+    std::memset(h.mats, 0, sizeof(h.mats));
+    for (uint32_t m = 0; m < h.nMats; ++m) h.mats[m] = scenes[i].materials[m];
+    defaultParams(h, h.params);
+    N += h.n;
+    C += h.numCells;
+  }
+  if (N >= 0x7fffffffull) return fail(XPBI_ERR_INVALID, "too many particles");
+  if (C >= 0x7fffffffull) return fail(XPBI_ERR_INVALID, "too many cells");
+  xpbi_sim* s = new xpbi_sim();
+  s->sc = std::move(sc);
+  int rc = XPBI_OK;
+  auto bail = [&](int code) {
+    destroyAll(s);
+    delete s;
+    return code;
+  };
+  if (cudaGetDevice(&s->device) != cudaSuccess) return bail(fail(XPBI_ERR_CUDA, "no CUDA device"));
+  if (cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&s->capture, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(XPBI_ERR_CUDA, "cudaStreamCreate failed"));
+  s->stream = s->own;
+  Bufs& b = s->b;
+  b.N = (uint32_t)N;
+  b.C = (uint32_t)C;
+  b.S = nScenes;
+  b.scanTiles = scan_tiles(b.C);
+  const size_t n = std::max<size_t>(b.N, 1);
+#define A(ptr, cnt)                               \
+  do {                                            \
+    rc = alloc(s, &(ptr), (cnt));                 \
+    if (rc != XPBI_OK) return bail(rc);           \
+  } while (0)
+  A(b.pos, n);
+  A(b.vel, n);
+  A(b.F, 9 * n);
+  A(b.state, n);
+  A(b.posS, n);
+  A(b.velS[0], n);
+  A(b.velS[1], n);
+  A(b.FS, 9 * n);
+  A(b.stateS, n);
+  A(b.L, 9 * n);
+  A(b.lam, n);
+  A(b.pbfLam, n);
+  A(b.Sp, 3 * n);
+  A(b.key, n);
+  A(b.tmp, n);
+  A(b.sortedIdx, n);
+  A(b.cursor, (size_t)b.C + 4);
+  A(b.cellStart, (size_t)b.C + 4);
+  unsigned long long* ctl = nullptr;
+  A(ctl, (size_t)b.scanTiles + 1);
+  b.tileTicket = reinterpret_cast<uint32_t*>(ctl);
+  b.bigCount = reinterpret_cast<uint32_t*>(ctl) + 1;
+  b.tileStatus = ctl + 1;
+  A(b.bigList, n / 64 + 2);
+  A(b.sceneOf, n);
+  A(b.scenes, nScenes);
+  A(b.mats, (size_t)nScenes * kMaxMats);
+  A(b.err, 1);
+  A(s->matWords, (size_t)nScenes * kMaxMats * XPBI_MATERIAL_WORDS);
+#undef A
+  // initial state (sim.js:52-81)
+  std::vector<float4> pos(n), vel(n);
+  std::vector<float> F(9 * n, 0.f), state(n, 0.f), zero(n, 0.f);
+  std::vector<uint16_t> sceneOf(n, 0);
+  for (uint32_t si = 0; si < nScenes; ++si) {
+    const xpbi_scene_desc& d = scenes[si];
+    const SceneHost& h = s->sc[si];
+    for (uint32_t k = 0; k < d.n; ++k) {
+      const size_t i = h.pBase + k;
+      const float seed = d.color_seeds ? d.color_seeds[k] : 0.f;
+      pos[i] = make_float4(d.positions[3 * k], d.positions[3 * k + 1], d.positions[3 * k + 2],
+                           (float)d.mat_ids[k] + seed);
+      vel[i] = d.velocities ? make_float4(d.velocities[3 * k], d.velocities[3 * k + 1], d.velocities[3 * k + 2], 0.f)
+                            : make_float4(0.f, 0.f, 0.f, 0.f);
+      state[i] = d.states ? d.states[k] : 0.f;
+      sceneOf[i] = (uint16_t)si;
+    }
+  }
+  for (size_t i = 0; i < b.N; ++i) {
+    F[0 * n + i] = 1.f;  // plane (c=0,r=0)
+    F[4 * n + i] = 1.f;  // plane (c=1,r=1)
+    F[8 * n + i] = 1.f;  // plane (c=2,r=2)
+  }
+  auto H2D = [&](void* dst, const void* src, size_t bytes) {
+    return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+  };
+  bool ok = H2D(b.pos, pos.data(), 16 * n) && H2D(b.vel, vel.data(), 16 * n) && H2D(b.F, F.data(), 36 * n) &&
+            H2D(b.state, state.data(), 4 * n) && H2D(b.lam, zero.data(), 4 * n) &&
+            H2D(b.pbfLam, zero.data(), 4 * n) && H2D(b.sceneOf, sceneOf.data(), 2 * n) &&
+            cudaMemset(b.err, 0, sizeof(int)) == cudaSuccess && cudaMemset(b.L, 0, 36 * n) == cudaSuccess &&
+            cudaMemset(b.sortedIdx, 0, 4 * n) == cudaSuccess &&
+            cudaMemset(b.cellStart, 0, 4 * ((size_t)b.C + 4)) == cudaSuccess;
+  if (!ok) return bail(fail(XPBI_ERR_CUDA, "initial upload failed"));
+  rc = upload(s);
+  if (rc != XPBI_OK) return bail(rc);
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess) return bail(fail(XPBI_ERR_CUDA, "initial sync failed"));
+  *out = s;
+  return XPBI_OK;
+}
+
+int checkSim(const xpbi_sim* s) {
+  if (!s) return fail(XPBI_ERR_INVALID, "sim handle is NULL");
+  return XPBI_OK;
+}
+
+int applySchedule(xpbi_sim* s, int32_t iterations, int32_t hasWater) {
+  if (iterations >= 0) {
+    if (iterations > 100000) return fail(XPBI_ERR_INVALID, "iterations out of range");
+    for (SceneHost& h : s->sc) {
+      if (h.iterations != iterations || h.hasWater != (hasWater ? 1 : 0)) s->dirty = true;
+      h.iterations = iterations;
+      h.hasWater = hasWater ? 1 : 0;
+    }
+  }
+  return XPBI_OK;
+}
+
+int checkDeviceErr(xpbi_sim* s) {
+  int e = 0;
+  XPBI_CK(cudaMemcpyAsync(&e, s->b.err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  XPBI_CK(cudaStreamSynchronize(s->stream));
+  if (e) {
+    cudaMemsetAsync(s->b.err, 0, sizeof(int), s->stream);
+    cudaStreamSynchronize(s->stream);
+    char msg[96];
+    std::snprintf(msg, sizeof(msg), "device error word 0x%x (bounded wait expired in the prefix scan)", e);
+    return fail(XPBI_ERR_DEVICE, msg);
+  }
+  return XPBI_OK;
+}
+
+int ensureGraph(xpbi_sim* s, const Schedule& sch) {
+  const std::string key = sch.key();
+  if (s->gexec && key == s->gkey) return XPBI_OK;
+  if (s->gexec) {
+    cudaGraphExecDestroy(s->gexec);
+    s->gexec = nullptr;
+  }
+  if (s->graph) {
+    cudaGraphDestroy(s->graph);
+    s->graph = nullptr;
+  }
+  XPBI_CK(cudaStreamBeginCapture(s->capture, cudaStreamCaptureModeThreadLocal));
+  enqueueSubstep(s, sch, s->capture, nullptr);
+  cudaGraph_t g = nullptr;
+  XPBI_CK(cudaStreamEndCapture(s->capture, &g));
+  s->graph = g;
+  XPBI_CK(cudaGraphInstantiate(&s->gexec, g, 0));
+  s->gkey = key;
+  return XPBI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* xpbi_last_error(void) { return g_err.c_str(); }
+
+int xpbi_pack_uniforms(const xpbi_scene_desc* scene, const xpbi_params* params,
+                       uint32_t params_words[XPBI_PARAMS_WORDS],
+                       uint32_t material_words[XPBI_MAX_MATERIALS * XPBI_MATERIAL_WORDS]) {
+  XPBI_TRY(validateScene(scene));
+  if (!params_words || !material_words) return fail(XPBI_ERR_INVALID, "output words are NULL");
+  SceneHost h;
+  XPBI_TRY(sizeGrid(*scene, h));
+  h.n = scene->n;
+  if (params) h.params = *params;
+  else std::memset(&h.params, 0, sizeof(h.params));
+  packParams(h, h.params, params_words);
+  std::memset(material_words, 0, 4 * XPBI_MAX_MATERIALS * XPBI_MATERIAL_WORDS);
+  for (uint32_t m = 0; m < scene->n_materials; ++m) packMaterial(scene->materials[m], h.V0, material_words + 16 * m);
+  return XPBI_OK;
+}
+
+int xpbi_create(const xpbi_scene_desc* scene, xpbi_sim** out) { return createImpl(scene, 1, out); }
+
+int xpbi_batch_create(const xpbi_scene_desc* scenes, uint32_t n_scenes, xpbi_sim** out) {
+  if (!scenes) return fail(XPBI_ERR_INVALID, "scenes is NULL");
+  return createImpl(scenes, n_scenes, out);
+}
+
+void xpbi_destroy(xpbi_sim* sim) {
+  if (!sim) return;
+  cudaStreamSynchronize(sim->stream);
+  destroyAll(sim);
+  delete sim;
+}
+
+int xpbi_write_materials(xpbi_sim* sim, int32_t scene, const xpbi_material* materials, uint32_t n) {
+  XPBI_TRY(checkSim(sim));
+  if (!materials || n < 1 || n > (uint32_t)kMaxMats) return fail(XPBI_ERR_INVALID, "materials must be 1..8");
+  for (uint32_t i = 0; i < n; ++i)
+    if (materials[i].kind > XPBI_WATER) return fail(XPBI_ERR_INVALID, "material kind out of range");
+  if (scene >= (int32_t)sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
+  for (uint32_t s = 0; s < sim->sc.size(); ++s) {
+    if (scene >= 0 && (uint32_t)scene != s) continue;
+    if (n < sim->sc[s].nMats) return fail(XPBI_ERR_INVALID, "fewer materials than the scene references");
+    for (uint32_t m = 0; m < n; ++m) sim->sc[s].mats[m] = materials[m];
+    sim->sc[s].nMats = n;
+  }
+  sim->dirty = true;
+  return XPBI_OK;
+}
+
+int xpbi_write_params(xpbi_sim* sim, int32_t scene, const xpbi_params* params) {
+  XPBI_TRY(checkSim(sim));
+  if (!params) return fail(XPBI_ERR_INVALID, "params is NULL");
+  if (!(params->dt > 0.f) || !std::isfinite(params->dt)) return fail(XPBI_ERR_INVALID, "dt must be positive");
+  if (scene >= (int32_t)sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
+  for (uint32_t s = 0; s < sim->sc.size(); ++s) {
+    if (scene >= 0 && (uint32_t)scene != s) continue;
+    sim->sc[s].params = *params;
+  }
+  sim->dirty = true;
+  return XPBI_OK;
+}
+
+int xpbi_set_schedule(xpbi_sim* sim, int32_t scene, int32_t iterations, int32_t has_water) {
+  XPBI_TRY(checkSim(sim));
+  if (iterations < 0 || iterations > 100000) return fail(XPBI_ERR_INVALID, "iterations out of range");
+  if (scene >= (int32_t)sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
+  for (uint32_t s = 0; s < sim->sc.size(); ++s) {
+    if (scene >= 0 && (uint32_t)scene != s) continue;
+    sim->sc[s].iterations = iterations;
+    sim->sc[s].hasWater = has_water ? 1 : 0;
+  }
+  sim->dirty = true;
+  return XPBI_OK;
+}
+
+int xpbi_encode_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water) {
+  XPBI_TRY(checkSim(sim));
+  for (const SceneHost& h : sim->sc)
+    if (!(h.params.dt > 0.f)) return fail(XPBI_ERR_INVALID, "write_params must be called before stepping");
+  XPBI_TRY(applySchedule(sim, iterations, has_water));
+  XPBI_TRY(upload(sim));
+  if (sim->b.N == 0) return XPBI_OK;
+  enqueueSubstep(sim, schedule(sim), sim->stream, nullptr);
+  XPBI_CK(cudaGetLastError());
+  sim->fresh = false;
+  return XPBI_OK;
+}
+
+int xpbi_step(xpbi_sim* sim, int32_t substeps, int32_t iterations, int32_t has_water) {
+  XPBI_TRY(checkSim(sim));
+  if (substeps < 0) return fail(XPBI_ERR_INVALID, "substeps must be >= 0");
+  for (const SceneHost& h : sim->sc)
+    if (!(h.params.dt > 0.f)) return fail(XPBI_ERR_INVALID, "write_params must be called before stepping");
+  XPBI_TRY(applySchedule(sim, iterations, has_water));
+  XPBI_TRY(upload(sim));
+  if (sim->b.N == 0 || substeps == 0) return XPBI_OK;
+  XPBI_TRY(ensureGraph(sim, schedule(sim)));
+  for (int i = 0; i < substeps; ++i) XPBI_CK(cudaGraphLaunch(sim->gexec, sim->stream));
+  sim->fresh = false;
+  return XPBI_OK;
+}
+
+int xpbi_synchronize(xpbi_sim* sim) {
+  XPBI_TRY(checkSim(sim));
+  XPBI_CK(cudaStreamSynchronize(sim->stream));
+  return checkDeviceErr(sim);
+}
+
+int xpbi_set_stream(xpbi_sim* sim, void* cuda_stream) {
+  XPBI_TRY(checkSim(sim));
+  XPBI_CK(cudaStreamSynchronize(sim->stream));
+  sim->stream = cuda_stream ? (cudaStream_t)cuda_stream : sim->own;
+  return XPBI_OK;
+}
+
+int xpbi_read_state(xpbi_sim* sim, uint32_t scene, float* pos4, float* vel4, float* F12, float* L12, float* aux4,
+                    uint32_t* sorted_idx, uint32_t* cell_tab) {
+  XPBI_TRY(checkSim(sim));
+  if (scene >= sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
+  XPBI_TRY(xpbi_synchronize(sim));
+  const SceneHost& h = sim->sc[scene];
+  const Bufs& b = sim->b;
+  const size_t n = h.n, o = h.pBase, N = b.N;
+  if (n == 0) {
+    if (cell_tab) XPBI_CK(cudaMemcpy(cell_tab, b.cellStart + h.cellBase, 4 * (size_t)h.numCells, cudaMemcpyDeviceToHost));
+    return XPBI_OK;
+  }
+  std::vector<float4> v(n);
+  if (pos4) XPBI_CK(cudaMemcpy(pos4, b.pos + o, 16 * n, cudaMemcpyDeviceToHost));
+  XPBI_CK(cudaMemcpy(v.data(), b.vel + o, 16 * n, cudaMemcpyDeviceToHost));
+  if (vel4) std::memcpy(vel4, v.data(), 16 * n);
+  auto planes = [&](const float* src, float* dst12) -> int {
+    std::vector<float> t(9 * n);
+    for (int p = 0; p < 9; ++p)
+      XPBI_CK(cudaMemcpy(t.data() + p * n, src + p * N + o, 4 * n, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; ++i)
+      for (int c = 0; c < 3; ++c) {
+        for (int r = 0; r < 3; ++r) dst12[12 * i + 4 * c + r] = t[(3 * c + r) * n + i];
+        dst12[12 * i + 4 * c + 3] = 0.f;
+      }
+    return XPBI_OK;
+  };
+  if (F12) XPBI_TRY(planes(b.F, F12));
+  if (L12) XPBI_TRY(planes(b.L, L12));
+  if (aux4) {
+    std::vector<float> lam(n), st(n), pl(n);
+    XPBI_CK(cudaMemcpy(lam.data(), b.lam + o, 4 * n, cudaMemcpyDeviceToHost));
+    XPBI_CK(cudaMemcpy(st.data(), b.state + o, 4 * n, cudaMemcpyDeviceToHost));
+    XPBI_CK(cudaMemcpy(pl.data(), b.pbfLam + o, 4 * n, cudaMemcpyDeviceToHost));
+    const float V0 = (float)h.V0;
+    for (size_t i = 0; i < n; ++i) {
+      aux4[4 * i] = sim->fresh ? V0 : v[i].w;  // aux.x = V^n (== vel.w after a substep)
+      aux4[4 * i + 1] = lam[i];
+      aux4[4 * i + 2] = st[i];
+      aux4[4 * i + 3] = pl[i];
+    }
+  }
+  if (sorted_idx) {
+    XPBI_CK(cudaMemcpy(sorted_idx, b.sortedIdx + o, 4 * n, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; ++i) sorted_idx[i] -= (uint32_t)o;
+  }
+  if (cell_tab) {
+    XPBI_CK(cudaMemcpy(cell_tab, b.cellStart + h.cellBase, 4 * (size_t)h.numCells, cudaMemcpyDeviceToHost));
+    for (size_t c = 0; c < h.numCells; ++c) cell_tab[c] -= (uint32_t)o;
+  }
+  return XPBI_OK;
+}
+
+int xpbi_read_positions(xpbi_sim* sim, uint32_t scene, float* out_pos4) {
+  XPBI_TRY(checkSim(sim));
+  if (!out_pos4) return fail(XPBI_ERR_INVALID, "output is NULL");
+  if (scene >= sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
+  const SceneHost& h = sim->sc[scene];
+  if (h.n == 0) return XPBI_OK;
+  XPBI_CK(cudaMemcpyAsync(out_pos4, sim->b.pos + h.pBase, 16 * (size_t)h.n, cudaMemcpyDeviceToHost, sim->stream));
+  return xpbi_synchronize(sim);
+}
+
+int xpbi_read_velocities(xpbi_sim* sim, uint32_t scene, float* out_vel4) {
+  XPBI_TRY(checkSim(sim));
+  if (!out_vel4) return fail(XPBI_ERR_INVALID, "output is NULL");
+  if (scene >= sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
+  const SceneHost& h = sim->sc[scene];
+  if (h.n == 0) return XPBI_OK;
+  XPBI_CK(cudaMemcpyAsync(out_vel4, sim->b.vel + h.pBase, 16 * (size_t)h.n, cudaMemcpyDeviceToHost, sim->stream));
+  return xpbi_synchronize(sim);
+}
+
+int xpbi_write_state(xpbi_sim* sim, uint32_t scene, const float* pos4, const float* vel4, const float* F12,
+                     const float* aux4) {
+  XPBI_TRY(checkSim(sim));
+  if (scene >= sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
+  XPBI_CK(cudaStreamSynchronize(sim->stream));
+  const SceneHost& h = sim->sc[scene];
+  const Bufs& b = sim->b;
+  const size_t n = h.n, o = h.pBase, N = b.N;
+  if (n == 0) return XPBI_OK;
+  if (pos4) {
+    for (size_t i = 0; i < n; ++i) {
+      float w = pos4[4 * i + 3];
+      if (!(w >= 0.f) || (uint32_t)w >= h.nMats) return fail(XPBI_ERR_INVALID, "pos.w material index out of range");
+    }
+    XPBI_CK(cudaMemcpy(b.pos + o, pos4, 16 * n, cudaMemcpyHostToDevice));
+  }
+  if (vel4) XPBI_CK(cudaMemcpy(b.vel + o, vel4, 16 * n, cudaMemcpyHostToDevice));
+  if (F12) {
+    std::vector<float> t(n);
+    for (int c = 0; c < 3; ++c)
+      for (int r = 0; r < 3; ++r) {
+        for (size_t i = 0; i < n; ++i) t[i] = F12[12 * i + 4 * c + r];
+        XPBI_CK(cudaMemcpy(b.F + (3 * c + r) * N + o, t.data(), 4 * n, cudaMemcpyHostToDevice));
+      }
+  }
+  if (aux4) {
+    std::vector<float> lam(n), st(n), pl(n);
+    for (size_t i = 0; i < n; ++i) {
+      lam[i] = aux4[4 * i + 1];
+      st[i] = aux4[4 * i + 2];
+      pl[i] = aux4[4 * i + 3];
+    }
+    XPBI_CK(cudaMemcpy(b.lam + o, lam.data(), 4 * n, cudaMemcpyHostToDevice));
+    XPBI_CK(cudaMemcpy(b.state + o, st.data(), 4 * n, cudaMemcpyHostToDevice));
+    XPBI_CK(cudaMemcpy(b.pbfLam + o, pl.data(), 4 * n, cudaMemcpyHostToDevice));
+  }
+  sim->fresh = false;
+  return XPBI_OK;
+}
+
+int xpbi_read_uniforms(xpbi_sim* sim, uint32_t scene, uint32_t params_words[XPBI_PARAMS_WORDS],
+                       uint32_t material_words[XPBI_MAX_MATERIALS * XPBI_MATERIAL_WORDS]) {
+  XPBI_TRY(checkSim(sim));
+  if (scene >= sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
+  const SceneHost& h = sim->sc[scene];
+  if (params_words) packParams(h, h.params, params_words);
+  if (material_words) {
+    std::memset(material_words, 0, 4 * XPBI_MAX_MATERIALS * XPBI_MATERIAL_WORDS);
+    for (uint32_t m = 0; m < h.nMats; ++m) packMaterial(h.mats[m], h.V0, material_words + 16 * m);
+  }
+  return XPBI_OK;
+}
+
+int xpbi_info(xpbi_sim* sim, uint32_t* n_particles, uint32_t* n_cells, uint32_t* n_scenes, int32_t dims[3]) {
+  XPBI_TRY(checkSim(sim));
+  if (n_particles) *n_particles = sim->b.N;
+  if (n_cells) *n_cells = sim->b.C;
+  if (n_scenes) *n_scenes = sim->b.S;
+  if (dims)
+    for (int k = 0; k < 3; ++k) dims[k] = sim->sc[0].dims[k];
+  return XPBI_OK;
+}
+
+int xpbi_profile_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water, float* ms, int32_t cap,
+                         int32_t* count, char* labels, size_t labels_cap) {
+  XPBI_TRY(checkSim(sim));
+  for (const SceneHost& h : sim->sc)
+    if (!(h.params.dt > 0.f)) return fail(XPBI_ERR_INVALID, "write_params must be called before stepping");
+  XPBI_TRY(applySchedule(sim, iterations, has_water));
+  XPBI_TRY(upload(sim));
+  if (sim->b.N == 0) {
+    if (count) *count = 0;
+    return XPBI_OK;
+  }
+  std::vector<cudaEvent_t> ev;
+  std::vector<std::string> lab;
+  Recorder rec;
+  rec.ev = &ev;
+  rec.labels = &lab;
+  enqueueSubstep(sim, schedule(sim), sim->stream, &rec);
+  XPBI_CK(cudaGetLastError());
+  XPBI_CK(cudaStreamSynchronize(sim->stream));
+  sim->fresh = false;
+  std::string text;
+  const int nl = (int)lab.size();
+  for (int k = 0; k < nl; ++k) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+    if (ms && k < cap) ms[k] = t;
+    char line[96];
+    std::snprintf(line, sizeof(line), "%s: %.3fms\n", lab[k].c_str(), t);
+    text += line;
+  }
+  for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  if (count) *count = nl;
+  if (labels && labels_cap > 0) {
+    size_t m = std::min(labels_cap - 1, text.size());
+    std::memcpy(labels, text.data(), m);
+    labels[m] = 0;
+  }
+  return checkDeviceErr(sim);
+}
+
+int xpbi_device_ptrs(xpbi_sim* sim, void** pos4, void** vel4, void** materials) {
+  XPBI_TRY(checkSim(sim));
+  if (pos4) *pos4 = sim->b.pos;
+  if (vel4) *vel4 = sim->b.vel;
+  if (materials) *materials = sim->matWords;
+  return XPBI_OK;
+}
+
+int xpbi_launches_per_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t* out) {
+  XPBI_TRY(checkSim(sim));
+  if (!out) return fail(XPBI_ERR_INVALID, "out is NULL");
+  XPBI_TRY(applySchedule(sim, iterations, has_water));
+  *out = kernelsPerSubstep(schedule(sim));
+  return XPBI_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,112 @@
+// Internal types shared by the host API and the kernels of libxpbi.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace xpbi {
+
+constexpr int kMaxMats = 8;            // simkernels.js:19
+constexpr uint32_t kRowCap = 384u;     // simkernels.js:73
+constexpr uint32_t kKindSnow = 5u;
+constexpr uint32_t kKindWater = 6u;
+
+// Device error word bits.
+constexpr int kErrLookback = 1;        // decoupled look-back wait expired
+
+// One scene's uniforms plus constants derived from them on the host. Every
+// derived constant is formed in f32 with the operation order of the per-call
+// WGSL expression it replaces, so it is bit-identical to recomputing it.
+struct SceneDev {
+  float origin[3];
+  float cs;                 // cell size = support
+  int dims[3];
+  uint32_t numCells;
+  uint32_t cellBase;        // first global cell of this scene
+  uint32_t pBase;           // first global particle of this scene
+  uint32_t n;               // particles of this scene
+  uint32_t matBase;         // first global material (scene * 8)
+  float dmin[3];
+  float dt;
+  float dmax[3];
+  float h;
+  float grav[3];
+  float support;
+  float colPos[3];
+  float colR;
+  float colVel[3];
+  float colActive;
+  float V0, xsphC, omega, pbfEps;
+  float sCorrK, contactOmega, kDamp, support2;
+  float sigW;               // 21 / (16 pi h^3)            common.js:67
+  float poly6C;             // 315 / (64 pi H^9)           common.js:86
+  float spikyC;             // -45 / (pi H^6)              common.js:93
+  float w00;                // poly6(0)                    simkernels.js:416
+  float w0;                 // poly6(0.2 H)                simkernels.js:465
+  float alphaT;             // (1/V0)/(dt dt)              simkernels.js:302
+  float minD;               // 0.75 h                      simkernels.js:333
+  float vmaxCFL;            // 0.45 support / dt           simkernels.js:535
+  float dvCap;              // 0.2 support / dt            simkernels.js:361
+  int iterations;           // XPBI Jacobi iterations this substep
+  int pbfIterations;        // PBF passes (first k iterations)
+  int hasWater;
+  float pad[2];
+};
+
+struct MatDev {
+  float mu, lam, density;
+  uint32_t kind;
+  float p0, p1, p2, p3;
+  float boundFriction, mass;
+  float pad[2];
+};
+
+// Device buffers of one handle. "Current" arrays hold the state between
+// substeps in the cell order of the last substep; the "sorted" arrays are the
+// substep's working copies written by the reorder.
+struct Bufs {
+  float4* pos;          // [N] current positions, w = material + seed
+  float4* vel;          // [N] current velocities, w = V^n
+  float* F;             // [9][N] current F, plane (3c+r) holds F[c][r]
+  float* state;         // [N] current plastic state
+  float4* posS;         // [N] sorted positions
+  float4* velS[2];      // [N] Jacobi ping-pong velocities
+  float* FS;            // [9][N] sorted F
+  float* stateS;        // [N] sorted plastic state
+  float* L;             // [9][N] kernel-gradient correction
+  float* lam;           // [N] XPBI multiplier
+  float* pbfLam;        // [N] PBF multiplier
+  float4* Sp;           // [3N] dlam * G L columns, self dv in .w
+  uint32_t* key;        // [N] global cell of each current particle
+  uint32_t* tmp;        // [N] unordered cell-bucket fill
+  uint32_t* sortedIdx;  // [N] global previous index of each sorted slot
+  uint32_t* cursor;     // [C] per-cell fill cursor
+  uint32_t* cellStart;  // [C+1] exclusive cell starts, sentinel = N
+  uint32_t* tileTicket;            // word 0 of the scan control block
+  uint32_t* bigCount;              // word 1: crowded cells found by the scan
+  unsigned long long* tileStatus;  // [tiles] look-back descriptors (after the two words)
+  uint32_t* bigList;               // [N/64 + 2] crowded cells (> 64 members)
+  uint16_t* sceneOf;    // [N] scene of each particle slot (static)
+  SceneDev* scenes;     // [S]
+  MatDev* mats;         // [S * 8]
+  int* err;             // [1] device error word
+  uint32_t N, C, S;
+  uint32_t scanTiles;
+};
+
+// ---- launchers (sort.cu) ----
+void launch_count(const Bufs& b, cudaStream_t st);
+void launch_scan(const Bufs& b, cudaStream_t st);
+void launch_scatter(const Bufs& b, cudaStream_t st);
+void launch_reorder(const Bufs& b, cudaStream_t st);
+uint32_t scan_tiles(uint32_t cells);
+
+// ---- launchers (solve.cu) ----
+void launch_computeL(const Bufs& b, cudaStream_t st);
+void launch_solveA(const Bufs& b, int k, const float4* velIn, cudaStream_t st);
+void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, cudaStream_t st);
+void launch_pbfA(const Bufs& b, int k, const float4* velIn, cudaStream_t st);
+void launch_pbfB(const Bufs& b, int k, const float4* velIn, float4* velOut, cudaStream_t st);
+void launch_xsph(const Bufs& b, const float4* velIn, float4* velOut, cudaStream_t st);
+void launch_updateF_integrate(const Bufs& b, const float4* velIn, cudaStream_t st);
+
+}  // namespace xpbi
