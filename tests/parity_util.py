@@ -5,8 +5,14 @@ is read back, the oracle runs one substep from it, the GPU runs the same
 substep, and the two results are compared:
   - sort: cell table (cell starts after the scatter) and permutation
     bit-exact;
-  - particle state (pos, vel, F, L, aux): normwise relative error
-    max|gpu - oracle| / max|oracle| <= REL_TOL per field, FP32.
+  - particle state (pos, vel, F, L, V^n = aux.x, plastic state = aux.z):
+    normwise relative error max|gpu - oracle| / max|oracle| <= REL_TOL per
+    field, FP32;
+  - the solver's multipliers (XPBI lambda = aux.y, PBF lambda = aux.w):
+    <= MULT_TOL. The PBF multiplier is -C / (...) with C = rho/rho0 - 1, a
+    difference of two nearly equal f32 numbers: a rounding-level change of
+    rho shifts C by ~1e-7 absolute, which is ~1e-4 relative to the largest
+    C of a scene at rest. That conditioning, not the kernels, sets MULT_TOL.
 The error of both against the FP64 oracle of the same substep is reported.
 """
 from __future__ import annotations
@@ -14,7 +20,8 @@ from __future__ import annotations
 import numpy as np
 
 REL_TOL = 1e-4
-FIELDS = ("pos", "vel", "F", "L", "aux")
+MULT_TOL = 1e-3
+FIELDS = ("pos", "vel", "F", "L", "Vn", "state")
 
 
 def rel(a, b) -> float:
@@ -45,21 +52,29 @@ def run_pair(xp, O, scene, warm: int = 0, iterations=None, has_water=None, param
     return s0, s1, ref, ref64
 
 
+def _split(st):
+    out = {k: st[k] for k in ("pos", "vel", "F", "L")}
+    out["Vn"] = st["aux"][:, 0]
+    out["lambda"] = st["aux"][:, 1]
+    out["state"] = st["aux"][:, 2]
+    out["pbf_lambda"] = st["aux"][:, 3]
+    return out
+
+
 def compare(s1, ref, ref64=None, has_pbf: bool = False) -> dict:
     """Per-field errors; raises AssertionError on a parity failure."""
     report = {}
     assert np.array_equal(s1["cellTab"], ref["cellTab"]), "cell table differs"
     assert np.array_equal(s1["sortedIdx"], ref["sortedIdx"]), "sort permutation differs"
-    for f in FIELDS:
-        a, b = s1[f], ref[f]
-        if f == "aux" and not has_pbf:
-            a, b = a[:, :3], b[:, :3]
-        e = rel(a, b)
-        report[f] = e
-        if ref64 is not None:
-            b64 = ref64[f] if not (f == "aux" and not has_pbf) else ref64[f][:, :3]
-            report[f + "_gpu_vs_f64"] = rel(a, b64)
-            report[f + "_f32oracle_vs_f64"] = rel(b, b64)
+    a_, b_ = _split(s1), _split(ref)
+    c_ = _split(ref64) if ref64 is not None else None
+    mults = ("lambda", "pbf_lambda") if has_pbf else ("lambda",)
+    for f in FIELDS + mults:
+        report[f] = rel(a_[f], b_[f])
+        if c_ is not None:
+            report[f + "_gpu_vs_f64"] = rel(a_[f], c_[f])
+            report[f + "_f32oracle_vs_f64"] = rel(b_[f], c_[f])
     bad = {f: report[f] for f in FIELDS if report[f] > REL_TOL}
-    assert not bad, f"parity failure (normwise relative error > {REL_TOL}): {bad}"
+    bad.update({f: report[f] for f in mults if report[f] > MULT_TOL})
+    assert not bad, f"parity failure: {bad}"
     return report

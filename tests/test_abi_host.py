@@ -53,7 +53,7 @@ def test_pack_uniforms_matches_sim_js_layout(xp, built_lib):
     assert int(pw[28]) == len(sc["positions"])
     assert _f(pw, 29) == np.float32(h ** 3)
     assert _f(pw, 30) == np.float32(0.01) and _f(pw, 31) == np.float32(0.5)
-    assert _f(pw, 32) == np.float32(100.0) and _f(pw, 33) == np.float32(0.1)
+    assert _f(pw, 32) == np.float32(100.0) and _f(pw, 33) == np.float32(1e-4)
     assert _f(pw, 34) == np.float32(1.5) and _f(pw, 35) == np.float32(0.4) and _f(pw, 36) == np.float32(0.4)
     # materials, sim.js:84-99: mu, lam from E, nu in f64; mass = rho * V0
     E, nu = 2e5, 0.3

@@ -26,8 +26,9 @@ def test_sand_column_config(xp, oracle, built_lib, warm):
 
 def test_sand_column_after_collapse_starts(xp, oracle, built_lib):
     sc = xp.scenes.config_sand_column()
-    s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=60)
-    # by now the column is flowing: multipliers and plastic projection active
+    # the column free-falls (uniform velocity, grad v = 0) until its base
+    # reaches the floor after ~160 substeps; by 300 it is flowing
+    s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=300)
     assert np.abs(ref["aux"][:, 1]).max() > 0
     compare(s1, ref, ref64)
 

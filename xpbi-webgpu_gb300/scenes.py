@@ -252,8 +252,13 @@ def config_nacc_snowball(seed=0):
 
 def config_dam_breach(seed=0, scale=1.0):
     """Dam breach in a 2x1x1 m box at r=0.008: water 75x80x100 (600k, PBF
-    rho0=1000, eps=100, s_corr k=0.1) beside a DP sand dam 50x80x100 (400k,
-    phi=35, E=2e5, nu=0.3); 15 XPBI + 4 PBF iterations, dt=1e-4, 200 substeps.
+    rho0=1000, eps=100) beside a DP sand dam 50x80x100 (400k, phi=35, E=2e5,
+    nu=0.3); 15 XPBI + 4 PBF iterations, dt=1e-4, 200 substeps.
+
+    s_corr uses the reference's own k = 1e-4 (scenes.js:89). With k = 0.1 the
+    reference's correction, (lambda_i + lambda_j + s_corr) gradW * m / rho0
+    (simkernels.js:467), moves a pair ~0.8 m at this spacing and every
+    particle hits the CFL cap in the first substep.
     ``scale`` < 1 shrinks the z extent (fewer particles) for quick checks."""
     rng = np.random.default_rng(seed)
     r = 0.008
@@ -267,7 +272,7 @@ def config_dam_breach(seed=0, scale=1.0):
                 color=[0.85, 0.63, 0.28], boundFriction=0.5)
     water = dict(kind=WATER, E=100, nu=0.3, density=1000.0, color=[0.25, 0.55, 0.95], boundFriction=0.0)
     _finish(s, rng, pos, mid, st, [sand, water], True)
-    return _solver(s, 1e-4, 15, 200, pbfIterations=4, sCorrK=0.1, pbfEps=100.0)
+    return _solver(s, 1e-4, 15, 200, pbfIterations=4, sCorrK=1e-4, pbfEps=100.0)
 
 
 def config_batch(n_scenes=256, seed=0, n_lo=2000, n_hi=60000):
