@@ -126,7 +126,8 @@ def test_batched_scenes_match_single(xp, oracle, built_lib):
     for k, sc in enumerate(scenes):
         pw, mw = uni[k]
         ref = oracle.substep(pw, mw, states[k], iters[k], sc["hasWater"], -1)
-        compare(after[k], ref, has_pbf=sc["hasWater"])
+        ref64 = oracle.substep(pw, mw, states[k], iters[k], sc["hasWater"], -1, f64=True)
+        compare(after[k], ref, ref64, has_pbf=sc["hasWater"])
 
 
 def test_profile_substep_labels(xp, built_lib):
