@@ -210,6 +210,8 @@ void buildSceneDev(const SceneHost& s, uint32_t sceneIdx, SceneDev& d, MatDev* m
       d.w0 = d.poly6C * x * x * x;
     }
   }
+  d.invH = 1.f / h;
+  d.invW0 = 1.f / fmaxf(d.w0, 1e-12f);
   d.alphaT = (1.f / d.V0) / (dt * dt);
   d.minD = 0.75f * h;
   d.vmaxCFL = 0.45f * H / dt;
@@ -373,7 +375,7 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
   for (int k = 0; k < sch.K; ++k) {
     launch_solveA(b, k, b.velS[in], st);
     R.mark(st, "solveA");
-    launch_solveB(b, k, b.velS[in], b.velS[in ^ 1], st);
+    launch_solveB(b, k, b.velS[in], b.velS[in ^ 1], sch.pbf[k] != 0, st);
     R.mark(st, "solveB");
     in ^= 1;
     if (sch.pbf[k]) {
@@ -468,6 +470,11 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   b.tileStatus = ctl + 1;
   A(b.bigList, n / 64 + 2);
   A(b.sceneOf, n);
+  A(b.nbr, (size_t)kNbrCap * n);
+  A(b.nbrCount, n);
+  A(b.nbrP, (size_t)kNbrCap * n);
+  A(b.nbrPCount, n);
+  A(b.xc, n);
   A(b.scenes, nScenes);
   A(b.mats, (size_t)nScenes * kMaxMats);
   A(b.err, 1);

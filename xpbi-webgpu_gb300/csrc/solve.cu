@@ -1,8 +1,20 @@
 // Neighbour-gather kernels of the XPBI substep, one thread per particle slot
 // in cell order. Each restates one compute entry point of
-// web/js/shaders/simkernels.js (cited per kernel) with the same stencil walk
-// (dz outer, dy inner, candidates ascending over the row-merged range of
-// three x-adjacent cells, capped at 384) and the same f32 operation order.
+// web/js/shaders/simkernels.js (cited per kernel).
+//
+// Neighbour lists. Positions do not move between the reorder and the final
+// update, so the set of in-support neighbours (b != i, |x_i - x_b|^2 <
+// support^2) is the same for computeL, every solveA / solveB iteration, xsph
+// and updateF. computeL walks the reference stencil once (dz outer, dy inner,
+// candidates ascending over the row-merged range of three x-adjacent cells,
+// capped at 384, simkernels.js:62-74) and records the in-support neighbours in
+// that order, so every later pass sums over exactly the reference's terms in
+// the reference's order without rescanning ~216 candidates per particle.
+// Lists that do not fit kNbrCap fall back to the stencil walk.
+//
+// PBF passes test predicted positions x + dt v, which change every
+// iteration: pbfA walks the stencil once per pass, records the predicted
+// neighbours it uses, and pbfB iterates that record.
 //
 // Batched handles: every slot belongs to one scene (sceneOf); its grid, cell
 // table range, uniforms and material table come from that scene, and a
@@ -19,11 +31,11 @@ constexpr int kThreads = 128;
 
 struct Ctx {
   const SceneDev* __restrict__ scene;
-  const MatDev* __restrict__ mats;   // this scene's 8 materials
+  const MatDev* __restrict__ mats;  // this scene's 8 materials
 };
 
 __device__ __forceinline__ Ctx ctxOf(const Bufs& b, uint32_t i) {
-  uint32_t s = b.S > 1 ? (uint32_t)b.sceneOf[i] : 0u;
+  const uint32_t s = b.S > 1 ? (uint32_t)b.sceneOf[i] : 0u;
   const SceneDev* S = b.scenes + s;
   return Ctx{S, b.mats + S->matBase};
 }
@@ -31,16 +43,16 @@ __device__ __forceinline__ Ctx ctxOf(const Bufs& b, uint32_t i) {
 // material index stored as a float value in pos.w (simkernels.js:41-44)
 __device__ __forceinline__ uint32_t matOfW(float w) {
   if (!(w > 0.f)) return 0u;
-  uint32_t m = (uint32_t)w;
+  const uint32_t m = (uint32_t)w;
   return m > 7u ? 7u : m;
 }
-__device__ __forceinline__ bool isSolid(const MatDev* mats, uint32_t mi) { return mats[mi].kind != kKindWater; }
+__device__ __forceinline__ bool isWaterMat(const MatDev* mats, uint32_t mi) { return mats[mi].kind == kKindWater; }
 
 // Stencil walk over the 9 row-merged ranges (simkernels.js:62-74).
 template <class Body>
 __device__ __forceinline__ void forStencil(const SceneDev& S, const uint32_t* __restrict__ cellStart, V3 x,
                                            Body&& body) {
-  I3 cc = cellCoord(S, x);
+  const I3 cc = cellCoord(S, x);
   const int x0 = max(cc.x - 1, 0);
   const int x1 = min(cc.x + 1, S.dims[0] - 1);
 #pragma unroll 1
@@ -56,59 +68,67 @@ __device__ __forceinline__ void forStencil(const SceneDev& S, const uint32_t* __
       const uint32_t beg = cellStart[c0];
       const uint32_t end = min(cellStart[c2 + 1], beg + kRowCap);
 #pragma unroll 1
-      for (uint32_t bb = beg; bb < end; ++bb) body(bb);
+      for (uint32_t j = beg; j < end; ++j) body(j);
     }
   }
 }
 
-// velocityGradient (simkernels.js:224-245)
-__device__ __forceinline__ M3 velocityGradient(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi, V3 vi,
-                                               const float4* __restrict__ velIn) {
-  const SceneDev& S = *cx.scene;
-  const M3 Li = loadM(b.L, b.N, i);
-  M3 G = mzero();
-  forStencil(S, b.cellStart, xi, [&](uint32_t j) {
-    if (j == i) return;
-    const float4 pj = b.posS[j];
-    if (!isSolid(cx.mats, matOfW(pj.w))) return;
-    V3 dxv = xi - xyz(pj);
-    if (dot(dxv, dxv) < S.support2) {
-      V3 gt = mul(Li, kernelGradW(S, dxv));
-      float4 vb = velIn[j];
-      V3 dv = (xyz(vb) - vi) * vb.w;
-      G = madd(G, M3{{dv * gt.x, dv * gt.y, dv * gt.z}});
+// In-support neighbours of slot i in stencil order: body(j, jIsWater).
+template <class Body>
+__device__ __forceinline__ void forNbrs(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi, Body&& body) {
+  const uint32_t cnt = b.nbrCount[i];
+  if (cnt != kNbrOverflow) {
+    const uint32_t* __restrict__ p = b.nbr + i;
+#pragma unroll 1
+    for (uint32_t k = 0; k < cnt; ++k) {
+      const uint32_t e = __ldg(p + (size_t)k * b.N);
+      body(e & ~kWaterBit, (e & kWaterBit) != 0u);
     }
-  });
-  return G;
+  } else {
+    const SceneDev& S = *cx.scene;
+    forStencil(S, b.cellStart, xi, [&](uint32_t j) {
+      if (j == i) return;
+      const float4 pj = b.posS[j];
+      const V3 d = xi - xyz(pj);
+      if (dot(d, d) < S.support2) body(j, isWaterMat(cx.mats, matOfW(pj.w)));
+    });
+  }
 }
 
 // ---------------------------------------------------------------- computeL
-// simkernels.js:189-221
+// Bonet-Lok correction with SVD pseudo-inverse (simkernels.js:189-221); also
+// records the substep's neighbour list.
 __global__ void __launch_bounds__(kThreads) k_computeL(Bufs b) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
-  Ctx cx = ctxOf(b, i);
+  const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
   const float4* __restrict__ velIn = b.velS[0];
-  V3 xi = xyz(b.posS[i]);
+  const V3 xi = xyz(b.posS[i]);
   M3 A = mzero();
+  uint32_t cnt = 0;
+  uint32_t* __restrict__ out = b.nbr + i;
   forStencil(S, b.cellStart, xi, [&](uint32_t j) {
     if (j == i) return;
-    V3 pb = xyz(b.posS[j]);
-    V3 dxv = xi - pb;
+    const float4 pj = b.posS[j];
+    const V3 pb = xyz(pj);
+    const V3 dxv = xi - pb;
     if (dot(dxv, dxv) < S.support2) {
-      V3 g = kernelGradW(S, dxv);
-      V3 r = pb - xi;
-      M3 o = {{g * r.x, g * r.y, g * r.z}};
+      const V3 g = gradWFast(S, dxv);
+      const V3 r = pb - xi;
+      const M3 o = {{g * r.x, g * r.y, g * r.z}};
       A = madd(A, mscale(o, velIn[j].w));
+      if (cnt < kNbrCap) out[(size_t)cnt * b.N] = j | (isWaterMat(cx.mats, matOfW(pj.w)) ? kWaterBit : 0u);
+      ++cnt;
     }
   });
-  SVD s = svd3(A);
+  b.nbrCount[i] = cnt <= kNbrCap ? cnt : kNbrOverflow;
+  const SVD s = svd3Fast(A);
   const float tol = 0.2f;
   V3 inv = splat(0.f);
-  if (fabsf(s.sig.x) > tol) inv.x = 1.f / s.sig.x;
-  if (fabsf(s.sig.y) > tol) inv.y = 1.f / s.sig.y;
-  if (fabsf(s.sig.z) > tol) inv.z = 1.f / s.sig.z;
+  if (fabsf(s.sig.x) > tol) inv.x = __frcp_rn(s.sig.x);
+  if (fabsf(s.sig.y) > tol) inv.y = __frcp_rn(s.sig.y);
+  if (fabsf(s.sig.z) > tol) inv.z = __frcp_rn(s.sig.z);
   storeM(b.L, b.N, i, diagMul(s.V, inv, s.U));
 }
 
@@ -118,28 +138,77 @@ __device__ __forceinline__ void storeSp(float4* __restrict__ Sp, uint32_t i, con
   Sp[3 * (size_t)i + 2] = make_float4(m.c[2].x, m.c[2].y, m.c[2].z, s.z);
 }
 
+// velocityGradient (simkernels.js:224-245) over the neighbour list.
+__device__ __forceinline__ M3 velocityGradient(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi, V3 vi,
+                                               const float4* __restrict__ velIn) {
+  const SceneDev& S = *cx.scene;
+  const M3 Li = loadM(b.L, b.N, i);
+  M3 G = mzero();
+  forNbrs(b, cx, i, xi, [&](uint32_t j, bool water) {
+    if (water) return;
+    const V3 dxv = xi - xyz(b.posS[j]);
+    const V3 gt = mul(Li, gradWFast(S, dxv));
+    const float4 vb = velIn[j];
+    const V3 dv = (xyz(vb) - vi) * vb.w;
+    G = madd(G, M3{{dv * gt.x, dv * gt.y, dv * gt.z}});
+  });
+  return G;
+}
+
 // ---------------------------------------------------------------- solveA
-// Inelastic constraint pass A (simkernels.js:248-309)
+// Inelastic constraint pass A (simkernels.js:248-309) in one neighbour sweep.
+//
+// The reference sweeps the neighbours twice: once for grad v (to form the
+// trial F and the constraint gradient G L) and once for
+//   denom = sum_b |g_b|^2 / m_b + |sgrad|^2 / m_i,  sgrad = -sum_b g_b,
+//   cdot  = sum_b g_b . v_b + sgrad . v_i,           g_b = V_b (G L) gradW_b.
+// With gt_b = L gradW_b (the term grad v already uses) and M = (dC/dF) F^nT,
+// g_b = V_b M gt_b, so with the per-sweep sums
+//   s = sum_b V_b gt_b,  Q = sum_b (V_b^2 / m_b) gt_b gt_b^T,  grad v = sum_b V_b (v_b - v_i) gt_b^T
+// the second sweep reduces exactly to
+//   sgrad = -M s,  denom = <M^T M, Q> + |sgrad|^2 / m_i,  cdot = <M, grad v>.
+// (The last identity also removes the cancellation of the reference's
+// sum_b g_b . v_b against sgrad . v_i when the body moves as a whole.)
 __global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4* __restrict__ velIn) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
-  Ctx cx = ctxOf(b, i);
+  const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
   if (k >= S.iterations) return;
   const float4 pi = b.posS[i];
   const uint32_t mi = matOfW(pi.w);
-  if (!isSolid(cx.mats, mi)) return;  // water: Sp is never read
+  if (isWaterMat(cx.mats, mi)) return;  // water: Sp is never read
   const float st = b.stateS[i];
-  MatDev m = hardenedMat(cx.mats[mi], st);
+  const MatDev m = hardenedMat(cx.mats[mi], st);
   const V3 xi = xyz(pi);
   const float4 vi4 = velIn[i];
   const V3 vi = xyz(vi4);
+  const M3 Li = loadM(b.L, b.N, i);
+  M3 G = mzero();
+  V3 sv = splat(0.f);
+  float q00 = 0.f, q11 = 0.f, q22 = 0.f, q01 = 0.f, q02 = 0.f, q12 = 0.f;
+  forNbrs(b, cx, i, xi, [&](uint32_t j, bool water) {
+    if (water) return;
+    const float4 pj = b.posS[j];
+    const V3 gt = mul(Li, gradWFast(S, xi - xyz(pj)));
+    const float4 vb = velIn[j];
+    const V3 dv = (xyz(vb) - vi) * vb.w;
+    G = madd(G, M3{{dv * gt.x, dv * gt.y, dv * gt.z}});
+    sv = sv + gt * vb.w;
+    const float c = vb.w * vb.w / cx.mats[matOfW(pj.w)].mass;
+    const V3 cg = gt * c;
+    q00 += cg.x * gt.x;
+    q11 += cg.y * gt.y;
+    q22 += cg.z * gt.z;
+    q01 += cg.x * gt.y;
+    q02 += cg.x * gt.z;
+    q12 += cg.y * gt.z;
+  });
   const M3 Fn = loadM(b.FS, b.N, i);
-  const M3 gradV = velocityGradient(b, cx, i, xi, vi, velIn);
-  const M3 Ftr = mul(madd(mident(), mscale(gradV, S.dt)), Fn);
-  const SVD sv = svd3(Ftr);
+  const M3 Ftr = mul(madd(mident(), mscale(G, S.dt)), Fn);
+  const SVD sd = svd3Fast(Ftr);
   float stOut;
-  const V3 sig = returnMap(sv.sig, m, st, S.dt, stOut);
+  const V3 sig = returnMap(sd.sig, m, st, S.dt, stOut);
   const float psi = stvkPsi(sig, m.mu, m.lam);
   const float C = sqrtf(fmaxf(2.f * psi, 0.f));
   if (C < 1e-7f) {
@@ -147,26 +216,16 @@ __global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4
     return;
   }
   const V3 dpsi = stvkDPsi(sig, m.mu, m.lam);
-  const M3 Pk = diagMul(sv.U, dpsi / C, sv.V);
-  const M3 GL = mul(mul(Pk, transpose(Fn)), loadM(b.L, b.N, i));
-  float denom = 0.f, cdot = 0.f;
-  V3 sgrad = splat(0.f);
-  forStencil(S, b.cellStart, xi, [&](uint32_t j) {
-    if (j == i) return;
-    const float4 pj = b.posS[j];
-    const uint32_t mj = matOfW(pj.w);
-    if (!isSolid(cx.mats, mj)) return;
-    V3 dxv = xi - xyz(pj);
-    if (dot(dxv, dxv) < S.support2) {
-      float4 vb = velIn[j];
-      V3 gb = vb.w * mul(GL, kernelGradW(S, dxv));
-      denom = denom + dot(gb, gb) / cx.mats[mj].mass;
-      sgrad = sgrad - gb;
-      cdot = cdot + dot(gb, xyz(vb));
-    }
-  });
-  denom = denom + dot(sgrad, sgrad) / m.mass;
-  cdot = cdot + dot(sgrad, vi);
+  const M3 Pk = diagMul(sd.U, dpsi * __frcp_rn(C), sd.V);
+  const M3 Mm = mul(Pk, transpose(Fn));
+  const M3 GL = mul(Mm, Li);
+  const V3 sgrad = -mul(Mm, sv);
+  // <M^T M, Q> = sum over column pairs (a, b) of (M_a . M_b) Q_ab
+  const V3 c0 = Mm.c[0], c1 = Mm.c[1], c2 = Mm.c[2];
+  const float denomN = dot(c0, c0) * q00 + dot(c1, c1) * q11 + dot(c2, c2) * q22 +
+                       2.f * (dot(c0, c1) * q01 + dot(c0, c2) * q02 + dot(c1, c2) * q12);
+  const float denom = denomN + dot(sgrad, sgrad) / m.mass;
+  const float cdot = dot(Mm.c[0], G.c[0]) + dot(Mm.c[1], G.c[1]) + dot(Mm.c[2], G.c[2]);
   const float g = S.kDamp;
   const float lam0 = b.lam[i];
   const float dlam = S.omega * (-C - S.alphaT * lam0 - g * S.dt * cdot) / ((1.f + g) * denom + S.alphaT);
@@ -211,19 +270,25 @@ __device__ __forceinline__ V3 applyBoundary(const SceneDev& S, V3 xcIn, V3 vIn, 
 }
 
 // ---------------------------------------------------------------- solveB
-// Constraint dv gather + contact correction + boundaries (simkernels.js:315-366)
+// Constraint dv gather + contact correction + boundaries (simkernels.js:315-366).
+// When a PBF pass follows, also stores the predicted position x + dt v_out
+// that pbfA / pbfB would otherwise recompute for every candidate.
 __global__ void __launch_bounds__(kThreads) k_solveB(Bufs b, int k, const float4* __restrict__ velIn,
-                                                      float4* __restrict__ velOut) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+                                                      float4* __restrict__ velOut, int writeXc) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
-  Ctx cx = ctxOf(b, i);
+  const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
   const float4 vi4 = velIn[i];
+  const float4 pi = b.posS[i];
   if (k >= S.iterations) {
     velOut[i] = vi4;
+    if (writeXc) {
+      const V3 xc = xyz(pi) + S.dt * xyz(vi4);
+      b.xc[i] = make_float4(xc.x, xc.y, xc.z, pi.w);
+    }
     return;
   }
-  const float4 pi = b.posS[i];
   const uint32_t mi = matOfW(pi.w);
   const MatDev& m = cx.mats[mi];
   const V3 xi = xyz(pi);
@@ -235,25 +300,22 @@ __global__ void __launch_bounds__(kThreads) k_solveB(Bufs b, int k, const float4
     const V3 xci = xi + S.dt * xyz(vi4);
     const float minD = S.minD;
     const float massI = m.mass;
-    forStencil(S, b.cellStart, xi, [&](uint32_t j) {
-      if (j == i) return;
-      const float4 pj = b.posS[j];
-      const uint32_t mj = matOfW(pj.w);
-      if (!isSolid(cx.mats, mj)) return;
-      const V3 pb = xyz(pj);
+    forNbrs(b, cx, i, xi, [&](uint32_t j, bool water) {
+      if (water) return;
+      const V3 pb = xyz(b.posS[j]);
       const V3 dxp = pb - xi;
-      if (dot(dxp, dxp) < S.support2) {
-        const float4 a0 = b.Sp[3 * (size_t)j], a1 = b.Sp[3 * (size_t)j + 1], a2 = b.Sp[3 * (size_t)j + 2];
-        const M3 Sb = {{xyz(a0), xyz(a1), xyz(a2)}};
-        dv = dv + Vi * mul(Sb, kernelGradW(S, dxp));
-        const V3 xcb = pb + S.dt * xyz(velIn[j]);
-        const V3 dxc = xci - xcb;
-        const float dist = length(dxc);
-        if (dist < minD && dist > 1e-9f) {
-          const float mb = cx.mats[mj].mass;
-          const float w = mb / (massI + mb);
-          corr = corr + dxc / dist * ((minD - dist) * w);
-        }
+      const float4 a0 = b.Sp[3 * (size_t)j], a1 = b.Sp[3 * (size_t)j + 1], a2 = b.Sp[3 * (size_t)j + 2];
+      const M3 Sb = {{xyz(a0), xyz(a1), xyz(a2)}};
+      dv = dv + Vi * mul(Sb, gradWFast(S, dxp));
+      const V3 xcb = pb + S.dt * xyz(velIn[j]);
+      const V3 dxc = xci - xcb;
+      const float d2 = dot(dxc, dxc);
+      if (d2 < minD * minD && d2 > 1e-18f) {
+        const float rinv = rsqrtf(d2);
+        const float dist = d2 * rinv;
+        const float mb = cx.mats[matOfW(b.posS[j].w)].mass;
+        const float w = mb / (massI + mb);
+        corr = corr + dxc * (rinv * ((minD - dist) * w));
       }
     });
   }
@@ -263,6 +325,10 @@ __global__ void __launch_bounds__(kThreads) k_solveB(Bufs b, int k, const float4
   V3 v = xyz(vi4) + dvv + corr * (S.contactOmega / S.dt);
   v = applyBoundary(S, xi + S.dt * v, v, xi, m.boundFriction);
   velOut[i] = make_float4(v.x, v.y, v.z, vi4.w);
+  if (writeXc) {
+    const V3 xc = xi + S.dt * v;
+    b.xc[i] = make_float4(xc.x, xc.y, xc.z, pi.w);
+  }
 }
 
 __device__ __forceinline__ bool pbfActive(const SceneDev& S, int k) {
@@ -270,50 +336,66 @@ __device__ __forceinline__ bool pbfActive(const SceneDev& S, int k) {
 }
 
 // ---------------------------------------------------------------- pbfA
-// PBF density multiplier (simkernels.js:407-439)
-__global__ void __launch_bounds__(kThreads) k_pbfA(Bufs b, int k, const float4* __restrict__ velIn) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+// PBF density multiplier (simkernels.js:407-439). Walks the stencil around
+// the current cell with predicted positions and records, in order, the
+// predicted neighbours pbfB will use: all of them for water, water ones for
+// solids (simkernels.js:457-458).
+__global__ void __launch_bounds__(kThreads) k_pbfA(Bufs b, int k) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
-  Ctx cx = ctxOf(b, i);
+  const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
   if (!pbfActive(S, k)) return;
   const float4 pi = b.posS[i];
   const uint32_t mi = matOfW(pi.w);
-  if (isSolid(cx.mats, mi)) {
-    b.pbfLam[i] = 0.f;
-    return;
-  }
+  const bool iWater = isWaterMat(cx.mats, mi);
   const MatDev& m = cx.mats[mi];
   const float rho0 = m.density;
-  const V3 xn = xyz(pi);
-  const V3 xci = xn + S.dt * xyz(velIn[i]);
+  const float invRho0 = __frcp_rn(rho0);
+  const float4 xci4 = b.xc[i];
+  const V3 xci = xyz(xci4);
   float rho = m.mass * S.w00;
   V3 gradSum = splat(0.f);
   float grad2 = 0.f;
-  forStencil(S, b.cellStart, xn, [&](uint32_t j) {
+  uint32_t cnt = 0;
+  uint32_t* __restrict__ out = b.nbrP + i;
+  forStencil(S, b.cellStart, xyz(pi), [&](uint32_t j) {
     if (j == i) return;
-    const float4 pj = b.posS[j];
-    const V3 xcb = xyz(pj) + S.dt * xyz(velIn[j]);
-    const V3 dxv = xci - xcb;
-    if (dot(dxv, dxv) < S.support2) {
-      const float mb = cx.mats[matOfW(pj.w)].mass;
-      rho = rho + mb * kernelPoly6(S, length(dxv));
-      const V3 g = kernelSpikyGrad(S, dxv) * (mb / rho0);
-      gradSum = gradSum + g;
-      grad2 = grad2 + dot(g, g);
+    const float4 c = b.xc[j];
+    const uint32_t mj = matOfW(c.w);
+    const bool jWater = isWaterMat(cx.mats, mj);
+    if (!(iWater || jWater)) return;
+    const V3 dxv = xci - xyz(c);
+    const float r2 = dot(dxv, dxv);
+    if (r2 < S.support2) {
+      if (cnt < kNbrCap) out[(size_t)cnt * b.N] = j | (jWater ? kWaterBit : 0u);
+      ++cnt;
+      if (iWater) {
+        const float mb = cx.mats[mj].mass;
+        rho = rho + mb * poly6Fast(S, r2);
+        const V3 g = spikyGradFast(S, dxv, r2) * (mb * invRho0);
+        gradSum = gradSum + g;
+        grad2 = grad2 + dot(g, g);
+      }
     }
   });
-  const float C = fmaxf(rho / rho0 - 1.f, 0.f);
+  b.nbrPCount[i] = cnt <= kNbrCap ? cnt : kNbrOverflow;
+  if (!iWater) {
+    b.pbfLam[i] = 0.f;
+    return;
+  }
+  const float C = fmaxf(rho * invRho0 - 1.f, 0.f);
   b.pbfLam[i] = -C / (grad2 + dot(gradSum, gradSum) + S.pbfEps);
 }
 
 // ---------------------------------------------------------------- pbfB
-// PBF position correction with s_corr (simkernels.js:441-477)
+// PBF position correction with s_corr (simkernels.js:441-477) over pbfA's
+// record of predicted neighbours.
 __global__ void __launch_bounds__(kThreads) k_pbfB(Bufs b, int k, const float4* __restrict__ velIn,
                                                     float4* __restrict__ velOut) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
-  Ctx cx = ctxOf(b, i);
+  const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
   const float4 vi4 = velIn[i];
   if (!pbfActive(S, k)) {
@@ -322,29 +404,41 @@ __global__ void __launch_bounds__(kThreads) k_pbfB(Bufs b, int k, const float4* 
   }
   const float4 pi = b.posS[i];
   const uint32_t mi = matOfW(pi.w);
-  const V3 xn = xyz(pi);
-  const V3 xci = xn + S.dt * xyz(vi4);
+  const V3 xci = xyz(b.xc[i]);
   V3 dp = splat(0.f);
   const float li = b.pbfLam[i];
-  const bool iAmWater = !isSolid(cx.mats, mi);
-  const float w0 = fmaxf(S.w0, 1e-12f);
-  forStencil(S, b.cellStart, xn, [&](uint32_t j) {
-    if (j == i) return;
-    const float4 pj = b.posS[j];
-    const uint32_t mj = matOfW(pj.w);
-    const bool bWater = !isSolid(cx.mats, mj);
-    if (!(iAmWater || bWater)) return;
-    const V3 xcb = xyz(pj) + S.dt * xyz(velIn[j]);
-    const V3 dxv = xci - xcb;
-    if (dot(dxv, dxv) < S.support2) {
-      const MatDev& mw = cx.mats[bWater ? mj : mi];
-      const float lb = b.pbfLam[j];
-      const float w = kernelPoly6(S, length(dxv));
-      const float sCorr = -S.sCorrK * powf(w / w0, 4.f);
-      dp = dp + (li + lb + sCorr) * kernelSpikyGrad(S, dxv) * (mw.mass / mw.density);
+  const bool iWater = isWaterMat(cx.mats, mi);
+  const MatDev& mWi = cx.mats[mi];
+  auto body = [&](uint32_t j, bool jWater) {
+    const float4 c = b.xc[j];
+    const V3 dxv = xci - xyz(c);
+    const float r2 = dot(dxv, dxv);
+    const MatDev& mw = jWater ? cx.mats[matOfW(c.w)] : mWi;  // a water material
+    const float lb = b.pbfLam[j];
+    const float x = poly6Fast(S, r2) * S.invW0;
+    const float x2 = x * x;
+    const float sCorr = -S.sCorrK * (x2 * x2);
+    dp = dp + (li + lb + sCorr) * spikyGradFast(S, dxv, r2) * (mw.mass / mw.density);
+  };
+  const uint32_t cnt = b.nbrPCount[i];
+  if (cnt != kNbrOverflow) {
+    const uint32_t* __restrict__ p = b.nbrP + i;
+#pragma unroll 1
+    for (uint32_t q = 0; q < cnt; ++q) {
+      const uint32_t e = __ldg(p + (size_t)q * b.N);
+      body(e & ~kWaterBit, (e & kWaterBit) != 0u);
     }
-  });
-  const float scale = iAmWater ? 1.f : 0.5f;
+  } else {
+    forStencil(S, b.cellStart, xyz(pi), [&](uint32_t j) {
+      if (j == i) return;
+      const float4 c = b.xc[j];
+      const bool jWater = isWaterMat(cx.mats, matOfW(c.w));
+      if (!(iWater || jWater)) return;
+      const V3 d = xci - xyz(c);
+      if (dot(d, d) < S.support2) body(j, jWater);
+    });
+  }
+  const float scale = iWater ? 1.f : 0.5f;
   const V3 v = xyz(vi4) + dp * (scale / S.dt);
   velOut[i] = make_float4(v.x, v.y, v.z, vi4.w);
 }
@@ -353,28 +447,24 @@ __global__ void __launch_bounds__(kThreads) k_pbfB(Bufs b, int k, const float4* 
 // simkernels.js:480-507
 __global__ void __launch_bounds__(kThreads) k_xsph(Bufs b, const float4* __restrict__ velIn,
                                                     float4* __restrict__ velOut) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
-  Ctx cx = ctxOf(b, i);
+  const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
   const float4 pi = b.posS[i];
   const V3 xi = xyz(pi);
   const float4 vi4 = velIn[i];
   const V3 vi = xyz(vi4);
-  const bool iSolid = isSolid(cx.mats, matOfW(pi.w));
+  const bool iWater = isWaterMat(cx.mats, matOfW(pi.w));
   V3 acc = splat(0.f);
-  forStencil(S, b.cellStart, xi, [&](uint32_t j) {
-    if (j == i) return;
-    const float4 pj = b.posS[j];
-    if (isSolid(cx.mats, matOfW(pj.w)) != iSolid) return;
-    const V3 dxv = xi - xyz(pj);
-    if (dot(dxv, dxv) < S.support2) {
-      const float4 vb = velIn[j];
-      acc = acc + vb.w * (xyz(vb) - vi) * kernelW(S, length(dxv));
-    }
+  forNbrs(b, cx, i, xi, [&](uint32_t j, bool jWater) {
+    if (jWater != iWater) return;
+    const V3 dxv = xi - xyz(b.posS[j]);
+    const float4 vb = velIn[j];
+    acc = acc + vb.w * (xyz(vb) - vi) * kernelWFast(S, dot(dxv, dxv));
   });
   float c = S.xsphC;
-  if (!iSolid) c = S.xsphC * 10.f;
+  if (iWater) c = S.xsphC * 10.f;
   const V3 v = vi + c * acc;
   velOut[i] = make_float4(v.x, v.y, v.z, vi4.w);
 }
@@ -384,9 +474,9 @@ __global__ void __launch_bounds__(kThreads) k_xsph(Bufs b, const float4* __restr
 // clamp and position update (simkernels.js:528-542). Outputs go to the
 // "current" arrays, so neighbours still read the unclamped sorted inputs.
 __global__ void __launch_bounds__(kThreads) k_updateF_integrate(Bufs b, const float4* __restrict__ velIn) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
-  Ctx cx = ctxOf(b, i);
+  const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
   const float4 pi = b.posS[i];
   const uint32_t mi = matOfW(pi.w);
@@ -394,11 +484,11 @@ __global__ void __launch_bounds__(kThreads) k_updateF_integrate(Bufs b, const fl
   const float st = b.stateS[i];
   M3 Fn = loadM(b.FS, b.N, i);
   float stOut = st;
-  if (isSolid(cx.mats, mi)) {
-    MatDev m = hardenedMat(cx.mats[mi], st);
+  if (!isWaterMat(cx.mats, mi)) {
+    const MatDev m = hardenedMat(cx.mats[mi], st);
     const M3 gradV = velocityGradient(b, cx, i, xyz(pi), xyz(vi4), velIn);
     const M3 Ftr = mul(madd(mident(), mscale(gradV, S.dt)), Fn);
-    const SVD sv = svd3(Ftr);
+    const SVD sv = svd3Fast(Ftr);
     const V3 sig = returnMap(sv.sig, m, st, S.dt, stOut);
     Fn = diagMul(sv.U, safeSig(sig), sv.V);
   }
@@ -421,11 +511,12 @@ void launch_computeL(const Bufs& b, cudaStream_t st) { k_computeL<<<grid(b.N), k
 void launch_solveA(const Bufs& b, int k, const float4* velIn, cudaStream_t st) {
   k_solveA<<<grid(b.N), kThreads, 0, st>>>(b, k, velIn);
 }
-void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, cudaStream_t st) {
-  k_solveB<<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut);
+void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, cudaStream_t st) {
+  k_solveB<<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, writeXc ? 1 : 0);
 }
 void launch_pbfA(const Bufs& b, int k, const float4* velIn, cudaStream_t st) {
-  k_pbfA<<<grid(b.N), kThreads, 0, st>>>(b, k, velIn);
+  (void)velIn;  // predicted positions were stored by the preceding solveB
+  k_pbfA<<<grid(b.N), kThreads, 0, st>>>(b, k);
 }
 void launch_pbfB(const Bufs& b, int k, const float4* velIn, float4* velOut, cudaStream_t st) {
   k_pbfB<<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut);

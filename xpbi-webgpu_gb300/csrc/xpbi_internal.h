@@ -10,6 +10,10 @@ constexpr uint32_t kRowCap = 384u;     // simkernels.js:73
 constexpr uint32_t kKindSnow = 5u;
 constexpr uint32_t kKindWater = 6u;
 
+constexpr uint32_t kNbrCap = 64u;      // neighbour-list capacity per particle
+constexpr uint32_t kNbrOverflow = 0xffffffffu;
+constexpr uint32_t kWaterBit = 0x80000000u;
+
 // Device error word bits.
 constexpr int kErrLookback = 1;        // decoupled look-back wait expired
 
@@ -46,10 +50,11 @@ struct SceneDev {
   float minD;               // 0.75 h                      simkernels.js:333
   float vmaxCFL;            // 0.45 support / dt           simkernels.js:535
   float dvCap;              // 0.2 support / dt            simkernels.js:361
+  float invH;               // 1 / h
+  float invW0;              // 1 / max(w0, 1e-12)          simkernels.js:466
   int iterations;           // XPBI Jacobi iterations this substep
   int pbfIterations;        // PBF passes (first k iterations)
   int hasWater;
-  float pad[2];
 };
 
 struct MatDev {
@@ -86,6 +91,11 @@ struct Bufs {
   unsigned long long* tileStatus;  // [tiles] look-back descriptors (after the two words)
   uint32_t* bigList;               // [N/64 + 2] crowded cells (> 64 members)
   uint16_t* sceneOf;    // [N] scene of each particle slot (static)
+  uint32_t* nbr;        // [kNbrCap][N] in-support neighbours, stencil order: index | water << 31
+  uint32_t* nbrCount;   // [N] list length, kNbrOverflow if it did not fit
+  uint32_t* nbrP;       // [kNbrCap][N] predicted-position neighbours of the current PBF pass
+  uint32_t* nbrPCount;  // [N]
+  float4* xc;           // [N] predicted positions x + dt v of the current PBF pass, w = pos.w
   SceneDev* scenes;     // [S]
   MatDev* mats;         // [S * 8]
   int* err;             // [1] device error word
@@ -103,7 +113,7 @@ uint32_t scan_tiles(uint32_t cells);
 // ---- launchers (solve.cu) ----
 void launch_computeL(const Bufs& b, cudaStream_t st);
 void launch_solveA(const Bufs& b, int k, const float4* velIn, cudaStream_t st);
-void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, cudaStream_t st);
+void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, cudaStream_t st);
 void launch_pbfA(const Bufs& b, int k, const float4* velIn, cudaStream_t st);
 void launch_pbfB(const Bufs& b, int k, const float4* velIn, float4* velOut, cudaStream_t st);
 void launch_xsph(const Bufs& b, const float4* velIn, float4* velOut, cudaStream_t st);

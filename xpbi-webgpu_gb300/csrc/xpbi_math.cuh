@@ -108,6 +108,41 @@ __device__ __forceinline__ V3 kernelSpikyGrad(const SceneDev& S, V3 dxv) {
   return dxv * (S.spikyC * t * t / r);
 }
 
+// Same kernels with the square root and the divisions by h and r replaced
+// by one reciprocal square root and multiplications by the precomputed 1/h:
+// a few ulp from the WGSL expressions, far below the parity tolerance.
+// r < 1e-9 (the reference's zero-distance guard) is r^2 < 1e-18.
+__device__ __forceinline__ V3 gradWFast(const SceneDev& S, V3 dxv) {
+  const float r2 = dot(dxv, dxv);
+  if (r2 < 1e-18f) return splat(0.f);
+  const float rinv = rsqrtf(r2);
+  const float q = r2 * rinv * S.invH;
+  if (q >= 2.f) return splat(0.f);
+  const float t = 1.f - 0.5f * q;
+  const float dwdq = S.sigW * (-5.f * q) * t * t * t;
+  return dxv * (dwdq * S.invH * rinv);
+}
+__device__ __forceinline__ float kernelWFast(const SceneDev& S, float r2) {
+  const float q = r2 > 0.f ? r2 * rsqrtf(r2) * S.invH : 0.f;
+  if (q >= 2.f) return 0.f;
+  const float t = 1.f - 0.5f * q;
+  return S.sigW * t * t * t * t * (2.f * q + 1.f);
+}
+// poly6 from the squared distance: H^2 - r^2 with r^2 taken directly
+__device__ __forceinline__ float poly6Fast(const SceneDev& S, float r2) {
+  if (r2 >= S.support2) return 0.f;
+  const float x = S.support2 - r2;
+  return S.poly6C * x * x * x;
+}
+__device__ __forceinline__ V3 spikyGradFast(const SceneDev& S, V3 dxv, float r2) {
+  if (r2 < 1e-18f) return splat(0.f);
+  const float rinv = rsqrtf(r2);
+  const float r = r2 * rinv;
+  if (r >= S.support) return splat(0.f);
+  const float t = S.support - r;
+  return dxv * (S.spikyC * t * t * rinv);
+}
+
 // ----------------------------------------------------------------- grid
 // common.js:97-103. Saturating f32->i32 (NaN -> 0) before clamping.
 __device__ __forceinline__ int axisCell(float p, float o, float cs, int dim) {
@@ -207,6 +242,88 @@ __device__ __forceinline__ SVD svd3(const M3& F) {
     u1 = normalize(a);
   }
   V3 u2 = cross(u0, u1);
+  if (det(F) < 0.f) sig.z = -sig.z;
+  out.U = {{u0, u1, u2}};
+  out.sig = sig;
+  return out;
+}
+
+// The same Jacobi sweeps with approximate reciprocal, reciprocal square
+// root and division (MUFU based). Rotation angles differ from the IEEE
+// version by a few ulp; the decomposition converges to the same U, sigma, V
+// to ~1e-6 and the products used downstream (U diag V^T) agree to rounding.
+template <int p, int q>
+__device__ __forceinline__ void jacobiRotFast(M3& S, M3& V) {
+  const float Spq = S.c[q][p];
+  const float Spp = S.c[p][p];
+  const float Sqq = S.c[q][q];
+  if (fabsf(Spq) < 1e-12f) return;
+  const float tau = __fdividef(Sqq - Spp, 2.f * Spq);
+  const float h2 = 1.f + tau * tau;
+  const float root = h2 * rsqrtf(h2);
+  const float t = __fdividef(1.f, tau >= 0.f ? tau + root : tau - root);
+  const float c = rsqrtf(1.f + t * t);
+  const float s = t * c;
+  M3 Sn = S;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float Skp = S.c[p][k], Skq = S.c[q][k];
+    Sn.c[p][k] = c * Skp - s * Skq;
+    Sn.c[q][k] = s * Skp + c * Skq;
+  }
+  M3 S2 = Sn;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float Spk = Sn.c[k][p], Sqk = Sn.c[k][q];
+    S2.c[k][p] = c * Spk - s * Sqk;
+    S2.c[k][q] = s * Spk + c * Sqk;
+  }
+  S = S2;
+  M3 Vn = V;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float Vkp = V.c[p][k], Vkq = V.c[q][k];
+    Vn.c[p][k] = c * Vkp - s * Vkq;
+    Vn.c[q][k] = s * Vkp + c * Vkq;
+  }
+  V = Vn;
+}
+
+__device__ __forceinline__ V3 normalizeFast(V3 a) { return a * rsqrtf(dot(a, a)); }
+
+__device__ __forceinline__ SVD svd3Fast(const M3& F) {
+  M3 S = mul(transpose(F), F);
+  M3 V = mident();
+#pragma unroll 1
+  for (int sweep = 0; sweep < 6; ++sweep) {
+    jacobiRotFast<0, 1>(S, V);
+    jacobiRotFast<0, 2>(S, V);
+    jacobiRotFast<1, 2>(S, V);
+  }
+  V3 sig = v3(sqrtf(fmaxf(S.c[0].x, 0.f)), sqrtf(fmaxf(S.c[1].y, 0.f)), sqrtf(fmaxf(S.c[2].z, 0.f)));
+  V3 a0 = V.c[0], a1 = V.c[1], a2 = V.c[2];
+  if (sig.x < sig.y) { swapf(sig.x, sig.y); swapv(a0, a1); }
+  if (sig.x < sig.z) { swapf(sig.x, sig.z); swapv(a0, a2); }
+  if (sig.y < sig.z) { swapf(sig.y, sig.z); swapv(a1, a2); }
+  if (dot(cross(a0, a1), a2) < 0.f) a2 = -a2;
+  SVD out;
+  out.V = {{a0, a1, a2}};
+  V3 u0, u1;
+  const float eps = 1e-8f;
+  if (sig.x > eps) u0 = normalizeFast(mul(F, a0));
+  else u0 = v3(1.f, 0.f, 0.f);
+  if (sig.y > eps) {
+    const V3 Fv1 = mul(F, a1);
+    u1 = Fv1 - dot(Fv1, u0) * u0;
+    const float l2 = dot(u1, u1);
+    if (l2 > eps * eps) u1 = u1 * rsqrtf(l2);
+    else u1 = normalizeFast(cross(v3(0.f, 1.f, 0.f), u0) + splat(1e-4f));
+  } else {
+    V3 a = cross(u0, v3(0.f, 1.f, 0.f));
+    if (dot(a, a) < 1e-8f) a = cross(u0, v3(1.f, 0.f, 0.f));
+    u1 = normalizeFast(a);
+  }
+  const V3 u2 = cross(u0, u1);
   if (det(F) < 0.f) sig.z = -sig.z;
   out.U = {{u0, u1, u2}};
   out.sig = sig;
