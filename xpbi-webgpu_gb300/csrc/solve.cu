@@ -14,7 +14,15 @@
 //
 // PBF passes test predicted positions x + dt v, which change every
 // iteration: pbfA walks the stencil once per pass, records the predicted
-// neighbours it uses, and pbfB iterates that record.
+// neighbours, and both PBF kernels then iterate that record.
+//
+// Scans are two-phase: a branch-light candidate test that only records
+// indices, then a uniform pass over the record; list loops issue the gathers
+// of entry k+1 before the arithmetic of entry k. (The candidate-scan
+// versions ran with ~14 of 32 lanes active and stalled on gathers.)
+//
+// Sorted records carry the water flag in the sign bit of pos.w (pos.w is
+// material index + colour seed >= 0, so fabsf restores it exactly).
 //
 // Batched handles: every slot belongs to one scene (sceneOf); its grid, cell
 // table range, uniforms and material table come from that scene, and a
@@ -42,16 +50,26 @@ __device__ __forceinline__ Ctx ctxOf(const Bufs& b, uint32_t i) {
 
 // material index stored as a float value in pos.w (simkernels.js:41-44)
 __device__ __forceinline__ uint32_t matOfW(float w) {
+  w = fabsf(w);
   if (!(w > 0.f)) return 0u;
   const uint32_t m = (uint32_t)w;
   return m > 7u ? 7u : m;
 }
-__device__ __forceinline__ bool isWaterMat(const MatDev* mats, uint32_t mi) { return mats[mi].kind == kKindWater; }
+__device__ __forceinline__ bool waterW(float w) { return signbit(w); }
 
-// Stencil walk over the 9 row-merged ranges (simkernels.js:62-74).
-template <class Body>
-__device__ __forceinline__ void forStencil(const SceneDev& S, const uint32_t* __restrict__ cellStart, V3 x,
-                                           Body&& body) {
+struct PV {
+  float4 p, v;
+};
+
+template <class T>
+__device__ __forceinline__ T ldg(const T* p) {
+  return __ldg(p);
+}
+
+// Stencil walk over the 9 row-merged ranges (simkernels.js:62-74):
+// row(beg, end) is called per in-range row.
+template <class Row>
+__device__ __forceinline__ void forRows(const SceneDev& S, const uint32_t* __restrict__ cellStart, V3 x, Row&& row) {
   const I3 cc = cellCoord(S, x);
   const int x0 = max(cc.x - 1, 0);
   const int x1 = min(cc.x + 1, S.dims[0] - 1);
@@ -65,64 +83,101 @@ __device__ __forceinline__ void forStencil(const SceneDev& S, const uint32_t* __
       if (y < 0 || y >= S.dims[1]) continue;
       const uint32_t c0 = S.cellBase + cellIndex(S, x0, y, z);
       const uint32_t c2 = S.cellBase + cellIndex(S, x1, y, z);
-      const uint32_t beg = cellStart[c0];
-      const uint32_t end = min(cellStart[c2 + 1], beg + kRowCap);
-#pragma unroll 1
-      for (uint32_t j = beg; j < end; ++j) body(j);
+      const uint32_t beg = __ldg(cellStart + c0);
+      const uint32_t end = min(__ldg(cellStart + c2 + 1), beg + kRowCap);
+      row(beg, end);
     }
   }
 }
 
-// In-support neighbours of slot i in stencil order: body(j, jIsWater).
-template <class Body>
-__device__ __forceinline__ void forNbrs(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi, Body&& body) {
+// Iterates a recorded list with the gather of entry k+1 issued before the
+// body of entry k runs.
+template <class Gather, class Body>
+__device__ __forceinline__ void forList(const uint32_t* __restrict__ list, uint32_t N, uint32_t cnt, Gather&& gather,
+                                        Body&& body) {
+  if (cnt == 0) return;
+  uint32_t e = __ldg(list);
+  auto d = gather(e & ~kWaterBit);
+#pragma unroll 1
+  for (uint32_t k = 1; k < cnt; ++k) {
+    const uint32_t en = __ldg(list + (size_t)k * N);
+    auto dn = gather(en & ~kWaterBit);
+    body(e & ~kWaterBit, (e & kWaterBit) != 0u, d);
+    e = en;
+    d = dn;
+  }
+  body(e & ~kWaterBit, (e & kWaterBit) != 0u, d);
+}
+
+// In-support neighbours of slot i in stencil order: body(j, jIsWater, data).
+template <class Gather, class Body>
+__device__ __forceinline__ void forNbrs(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi, Gather&& gather,
+                                        Body&& body) {
   const uint32_t cnt = b.nbrCount[i];
   if (cnt != kNbrOverflow) {
-    const uint32_t* __restrict__ p = b.nbr + i;
-#pragma unroll 1
-    for (uint32_t k = 0; k < cnt; ++k) {
-      const uint32_t e = __ldg(p + (size_t)k * b.N);
-      body(e & ~kWaterBit, (e & kWaterBit) != 0u);
-    }
+    forList(b.nbr + i, b.N, cnt, gather, body);
   } else {
     const SceneDev& S = *cx.scene;
-    forStencil(S, b.cellStart, xi, [&](uint32_t j) {
-      if (j == i) return;
-      const float4 pj = b.posS[j];
-      const V3 d = xi - xyz(pj);
-      if (dot(d, d) < S.support2) body(j, isWaterMat(cx.mats, matOfW(pj.w)));
+    forRows(S, b.cellStart, xi, [&](uint32_t beg, uint32_t end) {
+#pragma unroll 1
+      for (uint32_t j = beg; j < end; ++j) {
+        if (j == i) continue;
+        const float4 pj = ldg(b.posS + j);
+        const V3 d = xi - xyz(pj);
+        if (dot(d, d) < S.support2) body(j, waterW(pj.w), gather(j));
+      }
     });
   }
 }
 
+// Records, in stencil order, the candidates j != i of the rows around `x`
+// whose test(j) holds: list entry j | water bit from flag(j).
+template <class Test>
+__device__ __forceinline__ uint32_t recordCandidates(const SceneDev& S, const uint32_t* __restrict__ cellStart, V3 x,
+                                                     uint32_t i, uint32_t* __restrict__ out, uint32_t N, Test&& test) {
+  uint32_t cnt = 0;
+  forRows(S, cellStart, x, [&](uint32_t beg, uint32_t end) {
+#pragma unroll 4
+    for (uint32_t j = beg; j < end; ++j) {
+      uint32_t e;
+      const bool ok = test(j, e) && j != i;
+      if (ok) {
+        if (cnt < kNbrCap) out[(size_t)cnt * N] = e;
+        ++cnt;
+      }
+    }
+  });
+  return cnt;
+}
+
 // ---------------------------------------------------------------- computeL
-// Bonet-Lok correction with SVD pseudo-inverse (simkernels.js:189-221); also
-// records the substep's neighbour list.
+// Bonet-Lok correction with SVD pseudo-inverse (simkernels.js:189-221); its
+// candidate walk records the substep's neighbour list.
 __global__ void __launch_bounds__(kThreads) k_computeL(Bufs b) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
+  const float4* __restrict__ posS = b.posS;
   const float4* __restrict__ velIn = b.velS[0];
-  const V3 xi = xyz(b.posS[i]);
-  M3 A = mzero();
-  uint32_t cnt = 0;
-  uint32_t* __restrict__ out = b.nbr + i;
-  forStencil(S, b.cellStart, xi, [&](uint32_t j) {
-    if (j == i) return;
-    const float4 pj = b.posS[j];
-    const V3 pb = xyz(pj);
-    const V3 dxv = xi - pb;
-    if (dot(dxv, dxv) < S.support2) {
-      const V3 g = gradWFast(S, dxv);
-      const V3 r = pb - xi;
-      const M3 o = {{g * r.x, g * r.y, g * r.z}};
-      A = madd(A, mscale(o, velIn[j].w));
-      if (cnt < kNbrCap) out[(size_t)cnt * b.N] = j | (isWaterMat(cx.mats, matOfW(pj.w)) ? kWaterBit : 0u);
-      ++cnt;
-    }
+  const V3 xi = xyz(posS[i]);
+  const float s2 = S.support2;
+  const uint32_t cnt = recordCandidates(S, b.cellStart, xi, i, b.nbr + i, b.N, [&](uint32_t j, uint32_t& e) {
+    const float4 p = ldg(posS + j);
+    const V3 d = xi - xyz(p);
+    e = j | (waterW(p.w) ? kWaterBit : 0u);
+    return dot(d, d) < s2;
   });
   b.nbrCount[i] = cnt <= kNbrCap ? cnt : kNbrOverflow;
+  M3 A = mzero();
+  forNbrs(b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
+          [&](uint32_t, bool, const PV& d) {
+            const V3 pb = xyz(d.p);
+            const V3 g = gradWFast(S, xi - pb);
+            const V3 r = pb - xi;
+            const M3 o = {{g * r.x, g * r.y, g * r.z}};
+            A = madd(A, mscale(o, d.v.w));
+          });
   const SVD s = svd3Fast(A);
   const float tol = 0.2f;
   V3 inv = splat(0.f);
@@ -142,16 +197,16 @@ __device__ __forceinline__ void storeSp(float4* __restrict__ Sp, uint32_t i, con
 __device__ __forceinline__ M3 velocityGradient(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi, V3 vi,
                                                const float4* __restrict__ velIn) {
   const SceneDev& S = *cx.scene;
+  const float4* __restrict__ posS = b.posS;
   const M3 Li = loadM(b.L, b.N, i);
   M3 G = mzero();
-  forNbrs(b, cx, i, xi, [&](uint32_t j, bool water) {
-    if (water) return;
-    const V3 dxv = xi - xyz(b.posS[j]);
-    const V3 gt = mul(Li, gradWFast(S, dxv));
-    const float4 vb = velIn[j];
-    const V3 dv = (xyz(vb) - vi) * vb.w;
-    G = madd(G, M3{{dv * gt.x, dv * gt.y, dv * gt.z}});
-  });
+  forNbrs(b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
+          [&](uint32_t, bool water, const PV& d) {
+            if (water) return;
+            const V3 gt = mul(Li, gradWFast(S, xi - xyz(d.p)));
+            const V3 dv = (xyz(d.v) - vi) * d.v.w;
+            G = madd(G, M3{{dv * gt.x, dv * gt.y, dv * gt.z}});
+          });
   return G;
 }
 
@@ -175,9 +230,10 @@ __global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4
   const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
   if (k >= S.iterations) return;
-  const float4 pi = b.posS[i];
+  const float4* __restrict__ posS = b.posS;
+  const float4 pi = posS[i];
+  if (waterW(pi.w)) return;  // water: Sp is never read
   const uint32_t mi = matOfW(pi.w);
-  if (isWaterMat(cx.mats, mi)) return;  // water: Sp is never read
   const float st = b.stateS[i];
   const MatDev m = hardenedMat(cx.mats[mi], st);
   const V3 xi = xyz(pi);
@@ -187,23 +243,23 @@ __global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4
   M3 G = mzero();
   V3 sv = splat(0.f);
   float q00 = 0.f, q11 = 0.f, q22 = 0.f, q01 = 0.f, q02 = 0.f, q12 = 0.f;
-  forNbrs(b, cx, i, xi, [&](uint32_t j, bool water) {
-    if (water) return;
-    const float4 pj = b.posS[j];
-    const V3 gt = mul(Li, gradWFast(S, xi - xyz(pj)));
-    const float4 vb = velIn[j];
-    const V3 dv = (xyz(vb) - vi) * vb.w;
-    G = madd(G, M3{{dv * gt.x, dv * gt.y, dv * gt.z}});
-    sv = sv + gt * vb.w;
-    const float c = vb.w * vb.w / cx.mats[matOfW(pj.w)].mass;
-    const V3 cg = gt * c;
-    q00 += cg.x * gt.x;
-    q11 += cg.y * gt.y;
-    q22 += cg.z * gt.z;
-    q01 += cg.x * gt.y;
-    q02 += cg.x * gt.z;
-    q12 += cg.y * gt.z;
-  });
+  forNbrs(b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
+          [&](uint32_t, bool water, const PV& d) {
+            if (water) return;
+            const V3 gt = mul(Li, gradWFast(S, xi - xyz(d.p)));
+            const float Vb = d.v.w;
+            const V3 dv = (xyz(d.v) - vi) * Vb;
+            G = madd(G, M3{{dv * gt.x, dv * gt.y, dv * gt.z}});
+            sv = sv + gt * Vb;
+            const float c = Vb * Vb / cx.mats[matOfW(d.p.w)].mass;
+            const V3 cg = gt * c;
+            q00 += cg.x * gt.x;
+            q11 += cg.y * gt.y;
+            q22 += cg.z * gt.z;
+            q01 += cg.x * gt.y;
+            q02 += cg.x * gt.z;
+            q12 += cg.y * gt.z;
+          });
   const M3 Fn = loadM(b.FS, b.N, i);
   const M3 Ftr = mul(madd(mident(), mscale(G, S.dt)), Fn);
   const SVD sd = svd3Fast(Ftr);
@@ -269,6 +325,10 @@ __device__ __forceinline__ V3 applyBoundary(const SceneDev& S, V3 xcIn, V3 vIn, 
   return vv;
 }
 
+struct SBData {
+  float4 p, v, s0, s1, s2;
+};
+
 // ---------------------------------------------------------------- solveB
 // Constraint dv gather + contact correction + boundaries (simkernels.js:315-366).
 // When a PBF pass follows, also stores the predicted position x + dt v_out
@@ -279,8 +339,10 @@ __global__ void __launch_bounds__(kThreads) k_solveB(Bufs b, int k, const float4
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
+  const float4* __restrict__ posS = b.posS;
+  const float4* __restrict__ Sp = b.Sp;
   const float4 vi4 = velIn[i];
-  const float4 pi = b.posS[i];
+  const float4 pi = posS[i];
   if (k >= S.iterations) {
     velOut[i] = vi4;
     if (writeXc) {
@@ -293,31 +355,34 @@ __global__ void __launch_bounds__(kThreads) k_solveB(Bufs b, int k, const float4
   const MatDev& m = cx.mats[mi];
   const V3 xi = xyz(pi);
   V3 dv = splat(0.f), corr = splat(0.f);
-  if (m.kind != kKindWater) {
-    const float4 s0 = b.Sp[3 * (size_t)i], s1 = b.Sp[3 * (size_t)i + 1], s2 = b.Sp[3 * (size_t)i + 2];
+  if (!waterW(pi.w)) {
+    const float4 s0 = Sp[3 * (size_t)i], s1 = Sp[3 * (size_t)i + 1], s2 = Sp[3 * (size_t)i + 2];
     dv = v3(s0.w, s1.w, s2.w);
     const float Vi = vi4.w;
     const V3 xci = xi + S.dt * xyz(vi4);
     const float minD = S.minD;
     const float massI = m.mass;
-    forNbrs(b, cx, i, xi, [&](uint32_t j, bool water) {
-      if (water) return;
-      const V3 pb = xyz(b.posS[j]);
-      const V3 dxp = pb - xi;
-      const float4 a0 = b.Sp[3 * (size_t)j], a1 = b.Sp[3 * (size_t)j + 1], a2 = b.Sp[3 * (size_t)j + 2];
-      const M3 Sb = {{xyz(a0), xyz(a1), xyz(a2)}};
-      dv = dv + Vi * mul(Sb, gradWFast(S, dxp));
-      const V3 xcb = pb + S.dt * xyz(velIn[j]);
-      const V3 dxc = xci - xcb;
-      const float d2 = dot(dxc, dxc);
-      if (d2 < minD * minD && d2 > 1e-18f) {
-        const float rinv = rsqrtf(d2);
-        const float dist = d2 * rinv;
-        const float mb = cx.mats[matOfW(b.posS[j].w)].mass;
-        const float w = mb / (massI + mb);
-        corr = corr + dxc * (rinv * ((minD - dist) * w));
-      }
-    });
+    forNbrs(b, cx, i, xi,
+            [&](uint32_t j) {
+              return SBData{ldg(posS + j), ldg(velIn + j), ldg(Sp + 3 * (size_t)j), ldg(Sp + 3 * (size_t)j + 1),
+                            ldg(Sp + 3 * (size_t)j + 2)};
+            },
+            [&](uint32_t, bool water, const SBData& d) {
+              if (water) return;
+              const V3 pb = xyz(d.p);
+              const M3 Sb = {{xyz(d.s0), xyz(d.s1), xyz(d.s2)}};
+              dv = dv + Vi * mul(Sb, gradWFast(S, pb - xi));
+              const V3 xcb = pb + S.dt * xyz(d.v);
+              const V3 dxc = xci - xcb;
+              const float d2 = dot(dxc, dxc);
+              if (d2 < minD * minD && d2 > 1e-18f) {
+                const float rinv = rsqrtf(d2);
+                const float dist = d2 * rinv;
+                const float mb = cx.mats[matOfW(d.p.w)].mass;
+                const float w = mb / (massI + mb);
+                corr = corr + dxc * (rinv * ((minD - dist) * w));
+              }
+            });
   }
   V3 dvv = dv / (m.mass * S.dt);
   const float dvl = length(dvv);
@@ -338,55 +403,68 @@ __device__ __forceinline__ bool pbfActive(const SceneDev& S, int k) {
 // ---------------------------------------------------------------- pbfA
 // PBF density multiplier (simkernels.js:407-439). Walks the stencil around
 // the current cell with predicted positions and records, in order, the
-// predicted neighbours pbfB will use: all of them for water, water ones for
-// solids (simkernels.js:457-458).
+// predicted neighbours of this pass: all of them for water, the water ones
+// for solids (the pairs pbfB uses, simkernels.js:457-458).
 __global__ void __launch_bounds__(kThreads) k_pbfA(Bufs b, int k) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
   if (!pbfActive(S, k)) return;
+  const float4* __restrict__ xcS = b.xc;
   const float4 pi = b.posS[i];
-  const uint32_t mi = matOfW(pi.w);
-  const bool iWater = isWaterMat(cx.mats, mi);
-  const MatDev& m = cx.mats[mi];
-  const float rho0 = m.density;
-  const float invRho0 = __frcp_rn(rho0);
-  const float4 xci4 = b.xc[i];
-  const V3 xci = xyz(xci4);
-  float rho = m.mass * S.w00;
-  V3 gradSum = splat(0.f);
-  float grad2 = 0.f;
-  uint32_t cnt = 0;
-  uint32_t* __restrict__ out = b.nbrP + i;
-  forStencil(S, b.cellStart, xyz(pi), [&](uint32_t j) {
-    if (j == i) return;
-    const float4 c = b.xc[j];
-    const uint32_t mj = matOfW(c.w);
-    const bool jWater = isWaterMat(cx.mats, mj);
-    if (!(iWater || jWater)) return;
-    const V3 dxv = xci - xyz(c);
-    const float r2 = dot(dxv, dxv);
-    if (r2 < S.support2) {
-      if (cnt < kNbrCap) out[(size_t)cnt * b.N] = j | (jWater ? kWaterBit : 0u);
-      ++cnt;
-      if (iWater) {
-        const float mb = cx.mats[mj].mass;
-        rho = rho + mb * poly6Fast(S, r2);
-        const V3 g = spikyGradFast(S, dxv, r2) * (mb * invRho0);
-        gradSum = gradSum + g;
-        grad2 = grad2 + dot(g, g);
-      }
-    }
+  const bool iWater = waterW(pi.w);
+  const V3 xci = xyz(xcS[i]);
+  const float s2 = S.support2;
+  const uint32_t cnt = recordCandidates(S, b.cellStart, xyz(pi), i, b.nbrP + i, b.N, [&](uint32_t j, uint32_t& e) {
+    const float4 c = ldg(xcS + j);
+    const V3 d = xci - xyz(c);
+    const bool jWater = waterW(c.w);
+    e = j | (jWater ? kWaterBit : 0u);
+    return (iWater || jWater) && dot(d, d) < s2;
   });
-  b.nbrPCount[i] = cnt <= kNbrCap ? cnt : kNbrOverflow;
+  const uint32_t stored = cnt <= kNbrCap ? cnt : kNbrOverflow;
+  b.nbrPCount[i] = stored;
   if (!iWater) {
     b.pbfLam[i] = 0.f;
     return;
   }
+  const MatDev& m = cx.mats[matOfW(pi.w)];
+  const float rho0 = m.density;
+  const float invRho0 = __frcp_rn(rho0);
+  float rho = m.mass * S.w00;
+  V3 gradSum = splat(0.f);
+  float grad2 = 0.f;
+  auto body = [&](uint32_t, bool, const float4& c) {
+    const V3 dxv = xci - xyz(c);
+    const float r2 = dot(dxv, dxv);
+    const float mb = cx.mats[matOfW(c.w)].mass;
+    rho = rho + mb * poly6Fast(S, r2);
+    const V3 g = spikyGradFast(S, dxv, r2) * (mb * invRho0);
+    gradSum = gradSum + g;
+    grad2 = grad2 + dot(g, g);
+  };
+  if (stored != kNbrOverflow) {
+    forList(b.nbrP + i, b.N, stored, [&](uint32_t j) { return ldg(xcS + j); }, body);
+  } else {
+    forRows(S, b.cellStart, xyz(pi), [&](uint32_t beg, uint32_t end) {
+#pragma unroll 1
+      for (uint32_t j = beg; j < end; ++j) {
+        if (j == i) continue;
+        const float4 c = ldg(xcS + j);
+        const V3 d = xci - xyz(c);
+        if (dot(d, d) < s2) body(j, waterW(c.w), c);
+      }
+    });
+  }
   const float C = fmaxf(rho * invRho0 - 1.f, 0.f);
   b.pbfLam[i] = -C / (grad2 + dot(gradSum, gradSum) + S.pbfEps);
 }
+
+struct PBData {
+  float4 c;
+  float lb;
+};
 
 // ---------------------------------------------------------------- pbfB
 // PBF position correction with s_corr (simkernels.js:441-477) over pbfA's
@@ -402,40 +480,39 @@ __global__ void __launch_bounds__(kThreads) k_pbfB(Bufs b, int k, const float4* 
     velOut[i] = vi4;
     return;
   }
+  const float4* __restrict__ xcS = b.xc;
+  const float* __restrict__ lam = b.pbfLam;
   const float4 pi = b.posS[i];
   const uint32_t mi = matOfW(pi.w);
-  const V3 xci = xyz(b.xc[i]);
+  const V3 xci = xyz(xcS[i]);
   V3 dp = splat(0.f);
-  const float li = b.pbfLam[i];
-  const bool iWater = isWaterMat(cx.mats, mi);
+  const float li = lam[i];
+  const bool iWater = waterW(pi.w);
   const MatDev& mWi = cx.mats[mi];
-  auto body = [&](uint32_t j, bool jWater) {
-    const float4 c = b.xc[j];
-    const V3 dxv = xci - xyz(c);
+  auto gather = [&](uint32_t j) { return PBData{ldg(xcS + j), ldg(lam + j)}; };
+  auto body = [&](uint32_t, bool jWater, const PBData& d) {
+    const V3 dxv = xci - xyz(d.c);
     const float r2 = dot(dxv, dxv);
-    const MatDev& mw = jWater ? cx.mats[matOfW(c.w)] : mWi;  // a water material
-    const float lb = b.pbfLam[j];
+    const MatDev& mw = jWater ? cx.mats[matOfW(d.c.w)] : mWi;  // a water material
     const float x = poly6Fast(S, r2) * S.invW0;
     const float x2 = x * x;
     const float sCorr = -S.sCorrK * (x2 * x2);
-    dp = dp + (li + lb + sCorr) * spikyGradFast(S, dxv, r2) * (mw.mass / mw.density);
+    dp = dp + (li + d.lb + sCorr) * spikyGradFast(S, dxv, r2) * (mw.mass / mw.density);
   };
   const uint32_t cnt = b.nbrPCount[i];
   if (cnt != kNbrOverflow) {
-    const uint32_t* __restrict__ p = b.nbrP + i;
-#pragma unroll 1
-    for (uint32_t q = 0; q < cnt; ++q) {
-      const uint32_t e = __ldg(p + (size_t)q * b.N);
-      body(e & ~kWaterBit, (e & kWaterBit) != 0u);
-    }
+    forList(b.nbrP + i, b.N, cnt, gather, body);
   } else {
-    forStencil(S, b.cellStart, xyz(pi), [&](uint32_t j) {
-      if (j == i) return;
-      const float4 c = b.xc[j];
-      const bool jWater = isWaterMat(cx.mats, matOfW(c.w));
-      if (!(iWater || jWater)) return;
-      const V3 d = xci - xyz(c);
-      if (dot(d, d) < S.support2) body(j, jWater);
+    forRows(S, b.cellStart, xyz(pi), [&](uint32_t beg, uint32_t end) {
+#pragma unroll 1
+      for (uint32_t j = beg; j < end; ++j) {
+        if (j == i) continue;
+        const float4 c = ldg(xcS + j);
+        const bool jWater = waterW(c.w);
+        if (!(iWater || jWater)) continue;
+        const V3 d = xci - xyz(c);
+        if (dot(d, d) < S.support2) body(j, jWater, gather(j));
+      }
     });
   }
   const float scale = iWater ? 1.f : 0.5f;
@@ -451,18 +528,19 @@ __global__ void __launch_bounds__(kThreads) k_xsph(Bufs b, const float4* __restr
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
-  const float4 pi = b.posS[i];
+  const float4* __restrict__ posS = b.posS;
+  const float4 pi = posS[i];
   const V3 xi = xyz(pi);
   const float4 vi4 = velIn[i];
   const V3 vi = xyz(vi4);
-  const bool iWater = isWaterMat(cx.mats, matOfW(pi.w));
+  const bool iWater = waterW(pi.w);
   V3 acc = splat(0.f);
-  forNbrs(b, cx, i, xi, [&](uint32_t j, bool jWater) {
-    if (jWater != iWater) return;
-    const V3 dxv = xi - xyz(b.posS[j]);
-    const float4 vb = velIn[j];
-    acc = acc + vb.w * (xyz(vb) - vi) * kernelWFast(S, dot(dxv, dxv));
-  });
+  forNbrs(b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
+          [&](uint32_t, bool jWater, const PV& d) {
+            if (jWater != iWater) return;
+            const V3 dxv = xi - xyz(d.p);
+            acc = acc + d.v.w * (xyz(d.v) - vi) * kernelWFast(S, dot(dxv, dxv));
+          });
   float c = S.xsphC;
   if (iWater) c = S.xsphC * 10.f;
   const V3 v = vi + c * acc;
@@ -484,7 +562,7 @@ __global__ void __launch_bounds__(kThreads) k_updateF_integrate(Bufs b, const fl
   const float st = b.stateS[i];
   M3 Fn = loadM(b.FS, b.N, i);
   float stOut = st;
-  if (!isWaterMat(cx.mats, mi)) {
+  if (!waterW(pi.w)) {
     const MatDev m = hardenedMat(cx.mats[mi], st);
     const M3 gradV = velocityGradient(b, cx, i, xyz(pi), xyz(vi4), velIn);
     const M3 Ftr = mul(madd(mident(), mscale(gradV, S.dt)), Fn);
@@ -500,7 +578,7 @@ __global__ void __launch_bounds__(kThreads) k_updateF_integrate(Bufs b, const fl
   b.vel[i] = make_float4(v.x, v.y, v.z, vi4.w);
   V3 x = xyz(pi) + S.dt * v;
   x = v3(clampf(x.x, S.dmin[0], S.dmax[0]), clampf(x.y, S.dmin[1], S.dmax[1]), clampf(x.z, S.dmin[2], S.dmax[2]));
-  b.pos[i] = make_float4(x.x, x.y, x.z, pi.w);
+  b.pos[i] = make_float4(x.x, x.y, x.z, fabsf(pi.w));
 }
 
 inline unsigned grid(uint32_t n) { return (unsigned)((n + kThreads - 1) / kThreads); }

@@ -234,7 +234,12 @@ __global__ void __launch_bounds__(kThreads) k_reorder(Bufs b) {
   }
   b.sortedIdx[s] = i;
   const SceneDev& S = b.scenes[sceneOfSlot(b, i)];
-  b.posS[s] = b.pos[i];
+  // sorted records carry the water flag in the sign bit of pos.w (>= 0)
+  const float4 pp = b.pos[i];
+  uint32_t mi = 0u;
+  if (pp.w > 0.f) mi = min((uint32_t)pp.w, 7u);
+  const bool water = b.mats[S.matBase + mi].kind == kKindWater;
+  b.posS[s] = make_float4(pp.x, pp.y, pp.z, water ? -pp.w : pp.w);
   M3 F = loadM(b.F, b.N, i);
   storeM(b.FS, b.N, s, F);
   float Vn = S.V0 * clampf(det(F), 0.1f, 10.f);
