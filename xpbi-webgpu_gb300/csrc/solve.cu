@@ -90,17 +90,30 @@ __device__ __forceinline__ void forRows(const SceneDev& S, const uint32_t* __res
   }
 }
 
-// Iterates a recorded list with the gather of entry k+1 issued before the
-// body of entry k runs.
+// A particle's list occupies kNbrCap consecutive words (16-byte aligned) and
+// is read four entries per load, one load ahead; the gather of entry k+1 is
+// issued before the body of entry k runs.
+__device__ __forceinline__ uint32_t lane4(const uint4& q, uint32_t s) {
+  return s == 0u ? q.x : (s == 1u ? q.y : (s == 2u ? q.z : q.w));
+}
+
 template <class Gather, class Body>
-__device__ __forceinline__ void forList(const uint32_t* __restrict__ list, uint32_t N, uint32_t cnt, Gather&& gather,
+__device__ __forceinline__ void forList(const uint32_t* __restrict__ list, uint32_t cnt, Gather&& gather,
                                         Body&& body) {
   if (cnt == 0) return;
-  uint32_t e = __ldg(list);
+  const uint4* __restrict__ L = reinterpret_cast<const uint4*>(list);
+  uint4 cur = __ldg(L);
+  uint4 nxt = cnt > 4u ? __ldg(L + 1) : cur;
+  uint32_t e = cur.x;
   auto d = gather(e & ~kWaterBit);
 #pragma unroll 1
   for (uint32_t k = 1; k < cnt; ++k) {
-    const uint32_t en = __ldg(list + (size_t)k * N);
+    const uint32_t sl = k & 3u;
+    if (sl == 0u) {
+      cur = nxt;
+      if (k + 4u < cnt) nxt = __ldg(L + (k >> 2) + 1);
+    }
+    const uint32_t en = lane4(cur, sl);
     auto dn = gather(en & ~kWaterBit);
     body(e & ~kWaterBit, (e & kWaterBit) != 0u, d);
     e = en;
@@ -109,13 +122,18 @@ __device__ __forceinline__ void forList(const uint32_t* __restrict__ list, uint3
   body(e & ~kWaterBit, (e & kWaterBit) != 0u, d);
 }
 
+__device__ __forceinline__ uint32_t* listOf(uint32_t* base, uint32_t i) { return base + (size_t)i * kNbrCap; }
+__device__ __forceinline__ const uint32_t* listOf(const uint32_t* base, uint32_t i) {
+  return base + (size_t)i * kNbrCap;
+}
+
 // In-support neighbours of slot i in stencil order: body(j, jIsWater, data).
 template <class Gather, class Body>
 __device__ __forceinline__ void forNbrs(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi, Gather&& gather,
                                         Body&& body) {
   const uint32_t cnt = b.nbrCount[i];
   if (cnt != kNbrOverflow) {
-    forList(b.nbr + i, b.N, cnt, gather, body);
+    forList(listOf(b.nbr, i), cnt, gather, body);
   } else {
     const SceneDev& S = *cx.scene;
     forRows(S, b.cellStart, xi, [&](uint32_t beg, uint32_t end) {
@@ -132,21 +150,31 @@ __device__ __forceinline__ void forNbrs(const Bufs& b, const Ctx& cx, uint32_t i
 
 // Records, in stencil order, the candidates j != i of the rows around `x`
 // whose test(j) holds: list entry j | water bit from flag(j).
+// Entries are gathered four at a time in a register and written with one
+// 16-byte store.
 template <class Test>
 __device__ __forceinline__ uint32_t recordCandidates(const SceneDev& S, const uint32_t* __restrict__ cellStart, V3 x,
-                                                     uint32_t i, uint32_t* __restrict__ out, uint32_t N, Test&& test) {
+                                                     uint32_t i, uint32_t* __restrict__ out, Test&& test) {
   uint32_t cnt = 0;
+  uint4 q = make_uint4(0u, 0u, 0u, 0u);
+  uint4* __restrict__ O = reinterpret_cast<uint4*>(out);
   forRows(S, cellStart, x, [&](uint32_t beg, uint32_t end) {
 #pragma unroll 4
     for (uint32_t j = beg; j < end; ++j) {
       uint32_t e;
       const bool ok = test(j, e) && j != i;
       if (ok) {
-        if (cnt < kNbrCap) out[(size_t)cnt * N] = e;
+        const uint32_t sl = cnt & 3u;
+        if (sl == 0u) q.x = e;
+        else if (sl == 1u) q.y = e;
+        else if (sl == 2u) q.z = e;
+        else q.w = e;
+        if (sl == 3u && cnt < kNbrCap) O[cnt >> 2] = q;
         ++cnt;
       }
     }
   });
+  if ((cnt & 3u) != 0u && cnt < kNbrCap) O[cnt >> 2] = q;
   return cnt;
 }
 
@@ -162,7 +190,7 @@ __global__ void __launch_bounds__(kThreads) k_computeL(Bufs b) {
   const float4* __restrict__ velIn = b.velS[0];
   const V3 xi = xyz(posS[i]);
   const float s2 = S.support2;
-  const uint32_t cnt = recordCandidates(S, b.cellStart, xi, i, b.nbr + i, b.N, [&](uint32_t j, uint32_t& e) {
+  const uint32_t cnt = recordCandidates(S, b.cellStart, xi, i, listOf(b.nbr, i), [&](uint32_t j, uint32_t& e) {
     const float4 p = ldg(posS + j);
     const V3 d = xi - xyz(p);
     e = j | (waterW(p.w) ? kWaterBit : 0u);
@@ -416,7 +444,7 @@ __global__ void __launch_bounds__(kThreads) k_pbfA(Bufs b, int k) {
   const bool iWater = waterW(pi.w);
   const V3 xci = xyz(xcS[i]);
   const float s2 = S.support2;
-  const uint32_t cnt = recordCandidates(S, b.cellStart, xyz(pi), i, b.nbrP + i, b.N, [&](uint32_t j, uint32_t& e) {
+  const uint32_t cnt = recordCandidates(S, b.cellStart, xyz(pi), i, listOf(b.nbrP, i), [&](uint32_t j, uint32_t& e) {
     const float4 c = ldg(xcS + j);
     const V3 d = xci - xyz(c);
     const bool jWater = waterW(c.w);
@@ -445,7 +473,7 @@ __global__ void __launch_bounds__(kThreads) k_pbfA(Bufs b, int k) {
     grad2 = grad2 + dot(g, g);
   };
   if (stored != kNbrOverflow) {
-    forList(b.nbrP + i, b.N, stored, [&](uint32_t j) { return ldg(xcS + j); }, body);
+    forList(listOf(b.nbrP, i), stored, [&](uint32_t j) { return ldg(xcS + j); }, body);
   } else {
     forRows(S, b.cellStart, xyz(pi), [&](uint32_t beg, uint32_t end) {
 #pragma unroll 1
@@ -501,7 +529,7 @@ __global__ void __launch_bounds__(kThreads) k_pbfB(Bufs b, int k, const float4* 
   };
   const uint32_t cnt = b.nbrPCount[i];
   if (cnt != kNbrOverflow) {
-    forList(b.nbrP + i, b.N, cnt, gather, body);
+    forList(listOf(b.nbrP, i), cnt, gather, body);
   } else {
     forRows(S, b.cellStart, xyz(pi), [&](uint32_t beg, uint32_t end) {
 #pragma unroll 1

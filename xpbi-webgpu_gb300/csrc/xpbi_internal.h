@@ -91,9 +91,9 @@ struct Bufs {
   unsigned long long* tileStatus;  // [tiles] look-back descriptors (after the two words)
   uint32_t* bigList;               // [N/64 + 2] crowded cells (> 64 members)
   uint16_t* sceneOf;    // [N] scene of each particle slot (static)
-  uint32_t* nbr;        // [kNbrCap][N] in-support neighbours, stencil order: index | water << 31
+  uint32_t* nbr;        // [N][kNbrCap] in-support neighbours, stencil order: index | water << 31
   uint32_t* nbrCount;   // [N] list length, kNbrOverflow if it did not fit
-  uint32_t* nbrP;       // [kNbrCap][N] predicted-position neighbours of the current PBF pass
+  uint32_t* nbrP;       // [N][kNbrCap] predicted-position neighbours of the current PBF pass
   uint32_t* nbrPCount;  // [N]
   float4* xc;           // [N] predicted positions x + dt v of the current PBF pass, w = pos.w
   SceneDev* scenes;     // [S]
