@@ -463,6 +463,7 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   A(b.sortedIdx, n);
   A(b.cursor, (size_t)b.C + 4);
   A(b.cellStart, (size_t)b.C + 4);
+  A(b.cellWater, (size_t)b.C + 16);
   unsigned long long* ctl = nullptr;
   A(ctl, (size_t)b.scanTiles + 1);
   b.tileTicket = reinterpret_cast<uint32_t*>(ctl);

@@ -150,31 +150,19 @@ __device__ __forceinline__ void forNbrs(const Bufs& b, const Ctx& cx, uint32_t i
 
 // Records, in stencil order, the candidates j != i of the rows around `x`
 // whose test(j) holds: list entry j | water bit from flag(j).
-// Entries are gathered four at a time in a register and written with one
-// 16-byte store.
 template <class Test>
 __device__ __forceinline__ uint32_t recordCandidates(const SceneDev& S, const uint32_t* __restrict__ cellStart, V3 x,
                                                      uint32_t i, uint32_t* __restrict__ out, Test&& test) {
   uint32_t cnt = 0;
-  uint4 q = make_uint4(0u, 0u, 0u, 0u);
-  uint4* __restrict__ O = reinterpret_cast<uint4*>(out);
   forRows(S, cellStart, x, [&](uint32_t beg, uint32_t end) {
 #pragma unroll 4
     for (uint32_t j = beg; j < end; ++j) {
       uint32_t e;
       const bool ok = test(j, e) && j != i;
-      if (ok) {
-        const uint32_t sl = cnt & 3u;
-        if (sl == 0u) q.x = e;
-        else if (sl == 1u) q.y = e;
-        else if (sl == 2u) q.z = e;
-        else q.w = e;
-        if (sl == 3u && cnt < kNbrCap) O[cnt >> 2] = q;
-        ++cnt;
-      }
+      if (ok && cnt < kNbrCap) out[cnt] = e;
+      cnt += ok ? 1u : 0u;
     }
   });
-  if ((cnt & 3u) != 0u && cnt < kNbrCap) O[cnt >> 2] = q;
   return cnt;
 }
 
@@ -442,6 +430,27 @@ __global__ void __launch_bounds__(kThreads) k_pbfA(Bufs b, int k) {
   const float4* __restrict__ xcS = b.xc;
   const float4 pi = b.posS[i];
   const bool iWater = waterW(pi.w);
+  if (!iWater) {
+    // a solid only pairs with water here; candidates come from its 27 cells,
+    // so with no water particle in them there is nothing to record
+    const I3 cc = cellCoord(S, xyz(pi));
+    bool near = false;
+#pragma unroll
+    for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+      for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int x = cc.x + dx, y = cc.y + dy, z = cc.z + dz;
+          if (x >= 0 && x < S.dims[0] && y >= 0 && y < S.dims[1] && z >= 0 && z < S.dims[2])
+            near |= __ldg(b.cellWater + S.cellBase + cellIndex(S, x, y, z)) != 0;
+        }
+    if (!near) {
+      b.nbrPCount[i] = 0u;
+      b.pbfLam[i] = 0.f;
+      return;
+    }
+  }
   const V3 xci = xyz(xcS[i]);
   const float s2 = S.support2;
   const uint32_t cnt = recordCandidates(S, b.cellStart, xyz(pi), i, listOf(b.nbrP, i), [&](uint32_t j, uint32_t& e) {

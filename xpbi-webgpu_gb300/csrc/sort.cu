@@ -47,8 +47,12 @@ __global__ void __launch_bounds__(kThreads) k_count(Bufs b) {
   uint32_t key = 0;
   if (active) {
     const SceneDev& S = b.scenes[sceneOfSlot(b, i)];
-    key = cellKey(S, b.pos[i]);
+    const float4 p = b.pos[i];
+    key = cellKey(S, p);
     b.key[i] = key;
+    uint32_t mi = 0u;
+    if (p.w > 0.f) mi = min((uint32_t)p.w, 7u);
+    if (b.mats[S.matBase + mi].kind == kKindWater) b.cellWater[key] = 1u;
   }
   unsigned mask = __ballot_sync(0xffffffffu, active);
   if (!active) return;
@@ -259,6 +263,7 @@ uint32_t scan_tiles(uint32_t cells) { return (cells + 1 + kScanTile - 1) / kScan
 
 void launch_count(const Bufs& b, cudaStream_t st) {
   cudaMemsetAsync(b.cursor, 0, sizeof(uint32_t) * b.C, st);
+  cudaMemsetAsync(b.cellWater, 0, b.C, st);
   k_count<<<grid(b.N, kThreads), kThreads, 0, st>>>(b);
 }
 void launch_scan(const Bufs& b, cudaStream_t st) {

@@ -86,6 +86,7 @@ struct Bufs {
   uint32_t* sortedIdx;  // [N] global previous index of each sorted slot
   uint32_t* cursor;     // [C] per-cell fill cursor
   uint32_t* cellStart;  // [C+1] exclusive cell starts, sentinel = N
+  uint8_t* cellWater;   // [C] 1 if the cell holds a water particle this substep
   uint32_t* tileTicket;            // word 0 of the scan control block
   uint32_t* bigCount;              // word 1: crowded cells found by the scan
   unsigned long long* tileStatus;  // [tiles] look-back descriptors (after the two words)
