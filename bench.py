@@ -32,15 +32,26 @@ METRIC = "particle-substeps/s at equal residual, learned warm-start vs plain, 1 
 UNIT = "particle-substeps/s"
 
 # Algorithmic bytes per particle for one launch of each kernel (compulsory
-# traffic, minimal layout): solveA reads pos 16, vel 16, F 36, L 36, state 4,
-# lambda 4 and writes lambda 4, Sp 48; solveB reads pos 16, vel 16, Sp 48 and
-# writes vel 16; pbfA reads pos 16, vel 16 and writes the PBF multiplier 4;
-# pbfB reads pos 16, vel 16, multiplier 4 and writes vel 16; computeL reads
-# pos 16, vel 16 and writes L 36; xsph reads pos, vel and writes vel 48;
-# updateF+integrate reads pos 16, vel 16, F 36, L 36, state 4 and writes pos,
-# vel, F, state 72 (148 + 64 minus the shared pos/vel reads).
-ALGO_BYTES = {"solveA": 164, "solveB": 96, "pbfA": 36, "pbfB": 52, "computeL": 68, "xsph": 48,
-              "updateF+integrate": 180, "reorder": 148, "count": 20, "fill": 8, "scan": 8}
+# traffic, minimal layout), as (solid particle, water particle):
+#   solveA  solid: reads pos 16, vel 16, F 36, L 36, state 4, lambda 4, writes
+#           lambda 4, Sp 48 = 164; water: reads pos 16 and exits.
+#   solveB  solid: reads pos 16, vel 16, Sp 48, writes vel 16 = 96; water:
+#           pos, vel in, vel out = 48.
+#   pbfA    pos 16, predicted position 16, writes the multiplier 4 = 36.
+#   pbfB    predicted position 16, multiplier 4, vel in 16, vel out 16 = 52.
+#   computeL pos 16, vel 16, writes L 36 = 68.   xsph pos, vel in, vel out = 48.
+#   updateF+integrate solid: reads pos 16, vel 16, F 36, L 36, state 4,
+#           writes pos 16, vel 16, F 36, state 4 = 180; water: no L = 144.
+ALGO_BYTES = {"solveA": (164, 16), "solveB": (96, 48), "pbfA": (36, 36), "pbfB": (52, 52),
+              "computeL": (68, 68), "xsph": (48, 48), "updateF+integrate": (180, 144),
+              "reorder": (148, 148), "count": (20, 20), "fill": (8, 8), "scan": (8, 8)}
+
+# DRAM bytes per particle per launch (dram__bytes_read.sum +
+# dram__bytes_write.sum over particles) from the committed ncu capture of the
+# current kernels on the 1M-particle dam breach
+# (profiles/stencil_kernels_lists_dam_breach_1M.md); the traffic of a launch
+# grows with the particle count, so the bench scales it by the workload's.
+NCU_TRAFFIC_PER_PARTICLE = {"solveB": 121.4, "solveA": 119.7, "pbfA": 101.8, "computeL": 229.5}
 
 
 def workload(name: str, rank: int = 0):
@@ -240,10 +251,17 @@ def run_xpbi(args, rank: int, world: int):
         peak_src = "measured"
     else:
         peak, peak_src = 6800.0, "fallback"
-    achieved = ALGO_BYTES.get(dom, 0) * n_total / (dom_avg_ms / 1e3) / 1e9
+    n_water = sum(int(sum(1 for m in s["matIds"] if s["materials"][m]["kind"] == 6)) for s in scenes)
+    n_solid = n_total - n_water
+    bs, bw = ALGO_BYTES.get(dom, (0, 0))
+    algo = bs * n_solid + bw * n_water  # bytes per launch
+    achieved = algo / (dom_avg_ms / 1e3) / 1e9
+    tpp = NCU_TRAFFIC_PER_PARTICLE.get(dom)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
-                "algo_bytes_per_particle": ALGO_BYTES.get(dom),
+                "frac": achieved / peak, "peak_source": peak_src,
+                "traffic": None if tpp is None else tpp * n_total,
+                "traffic_source": "ncu capture of the 1M-particle dam breach scaled by particle count",
+                "algo_bytes_per_launch": algo, "solid_particles": n_solid, "water_particles": n_water,
                 "share": sum(per[dom]) / total_ms,
                 "kernel_ms": {k: round(statistics.mean(v), 4) for k, v in per.items()}}
     sim.close()
