@@ -47,10 +47,9 @@ ALGO_BYTES = {"solveA": (164, 16), "solveB": (96, 48), "pbfA": (36, 36), "pbfB":
               "reorder": (148, 148), "count": (20, 20), "fill": (8, 8), "scan": (8, 8)}
 
 # DRAM bytes per particle per launch (dram__bytes_read.sum +
-# dram__bytes_write.sum over particles) from the committed ncu capture of the
-# current kernels on the 1M-particle dam breach
-# (profiles/stencil_kernels_lists_dam_breach_1M.md); the traffic of a launch
-# grows with the particle count, so the bench scales it by the workload's.
+# dram__bytes_write.sum over particles) from an ncu --set full capture of the
+# current kernels on the 1M-particle dam breach; the traffic of a launch grows
+# with the particle count, so the bench scales it by the workload's.
 NCU_TRAFFIC_PER_PARTICLE = {"solveB": 121.4, "solveA": 119.7, "pbfA": 101.8, "computeL": 229.5}
 
 

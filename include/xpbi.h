@@ -184,6 +184,25 @@ int xpbi_device_ptrs(xpbi_sim* sim, void** pos4, void** vel4, void** materials);
 /* Number of kernel launches one substep issues with this schedule. */
 int xpbi_launches_per_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t* out);
 
+/* ---- warm-start network (no counterpart in the reference) ----
+ * A per-particle MLP 16 -> 64 -> 64 -> 64 -> 1 (SiLU), BF16 weights, FP32
+ * accumulate, run on the tcgen05 tensor cores. Parameters are one f32 vector:
+ * W1[64][16] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] w4[64] b4. */
+int xpbi_mlp_param_count(void);
+
+/* y[r] = net(X[r]) for rows of 16 features (host buffers, synchronous). */
+int xpbi_mlp_forward(const float* X, uint32_t rows, const float* params, float* y);
+
+/* Gradient of the mean squared error (1/rows) sum_r (net(X[r]) - T[r])^2
+ * with respect to params; *loss (may be NULL) receives the error. */
+int xpbi_mlp_grad(const float* X, const float* T, uint32_t rows, const float* params, float* grad, float* loss);
+
+/* `steps` Adam steps (lr, betas 0.9 / 0.999) on consecutive mini-batches of
+ * `batch` rows, cycling through the rows in the given order; params is
+ * updated in place, loss_history (may be NULL) gets each step's loss. */
+int xpbi_mlp_train(const float* X, const float* T, uint32_t rows, float* params, int32_t steps, uint32_t batch,
+                   float lr, float* loss_history);
+
 #ifdef __cplusplus
 }
 #endif

@@ -26,6 +26,7 @@ EXPORTS = (
     "xpbi_step", "xpbi_synchronize", "xpbi_set_stream", "xpbi_read_positions",
     "xpbi_read_velocities", "xpbi_read_state", "xpbi_write_state", "xpbi_read_uniforms",
     "xpbi_info", "xpbi_profile_substep", "xpbi_device_ptrs", "xpbi_launches_per_substep",
+    "xpbi_mlp_param_count", "xpbi_mlp_forward", "xpbi_mlp_grad", "xpbi_mlp_train",
 )
 
 
@@ -87,6 +88,10 @@ _SIGS = {
                                        C.c_char_p, C.c_size_t]),
     "xpbi_device_ptrs": (C.c_int, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
     "xpbi_launches_per_substep": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
+    "xpbi_mlp_param_count": (C.c_int, []),
+    "xpbi_mlp_forward": (C.c_int, [_F32P, C.c_uint32, _F32P, _F32P]),
+    "xpbi_mlp_grad": (C.c_int, [_F32P, _F32P, C.c_uint32, _F32P, _F32P, _F32P]),
+    "xpbi_mlp_train": (C.c_int, [_F32P, _F32P, C.c_uint32, _F32P, C.c_int32, C.c_uint32, C.c_float, _F32P]),
 }
 
 

@@ -250,6 +250,10 @@ int validateScene(const xpbi_scene_desc* d) {
 
 }  // namespace
 
+namespace xpbi {
+int setError(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace xpbi
+
 struct xpbi_sim {
   int device = 0;
   cudaStream_t own = nullptr;
