@@ -184,6 +184,33 @@ int xpbi_device_ptrs(xpbi_sim* sim, void** pos4, void** vel4, void** materials);
 /* Number of kernel launches one substep issues with this schedule. */
 int xpbi_launches_per_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t* out);
 
+/* ---- solver modes (no counterpart in the reference) ----
+ * mode 0: the reference solve (every XPBI iteration starts from lambda = 0).
+ * mode 1: iteration 0 starts from the warm-start network's multiplier.
+ * mode 2: iteration 0 starts from the particle's previous-substep multiplier.
+ * rel_tol > 0: a scene stops iterating (its remaining passes skip) once its
+ *   constraint residual |C + alpha_tilde lambda| falls to rel_tol times
+ *   |C| at the predicted velocities; <= 0 keeps the fixed iteration count.
+ * track_residual: record the residual norm of every iteration and of the
+ *   final state (xpbi_read_residuals).
+ * log_features: compute the network features every substep
+ *   (xpbi_read_training). */
+int xpbi_set_solver(xpbi_sim* sim, int32_t mode, float rel_tol, int32_t track_residual, int32_t log_features);
+
+/* Load the warm-start network's 9473 parameters (layout of xpbi_mlp_*). */
+int xpbi_set_network(xpbi_sim* sim, const float* params, uint32_t count);
+
+/* Residual norms of the last substep of one scene: norms[0] = |C(v_pred)|,
+ * norms[1 + k] = |r_k| entering iteration k (NaN after an early stop),
+ * norms[1 + K] = |r| of the final state (with track_residual);
+ * *iterations_run = iterations whose update was applied. */
+int xpbi_read_residuals(xpbi_sim* sim, uint32_t scene, double* norms, int32_t cap, int32_t* iterations_run);
+
+/* Training rows of the last substep of one scene (cell-sorted order):
+ * features16 [n][16] (zeros for water), target [n] = alpha_tilde * final
+ * lambda, *alpha_tilde (may be NULL). Needs log_features or mode 1. */
+int xpbi_read_training(xpbi_sim* sim, uint32_t scene, float* features16, float* target, float* alpha_tilde);
+
 /* ---- warm-start network (no counterpart in the reference) ----
  * A per-particle MLP 16 -> 64 -> 64 -> 64 -> 1 (SiLU), BF16 weights, FP32
  * accumulate, run on the tcgen05 tensor cores. Parameters are one f32 vector:

@@ -27,6 +27,7 @@ EXPORTS = (
     "xpbi_read_velocities", "xpbi_read_state", "xpbi_write_state", "xpbi_read_uniforms",
     "xpbi_info", "xpbi_profile_substep", "xpbi_device_ptrs", "xpbi_launches_per_substep",
     "xpbi_mlp_param_count", "xpbi_mlp_forward", "xpbi_mlp_grad", "xpbi_mlp_train",
+    "xpbi_set_solver", "xpbi_set_network", "xpbi_read_residuals", "xpbi_read_training",
 )
 
 
@@ -92,6 +93,10 @@ _SIGS = {
     "xpbi_mlp_forward": (C.c_int, [_F32P, C.c_uint32, _F32P, _F32P]),
     "xpbi_mlp_grad": (C.c_int, [_F32P, _F32P, C.c_uint32, _F32P, _F32P, _F32P]),
     "xpbi_mlp_train": (C.c_int, [_F32P, _F32P, C.c_uint32, _F32P, C.c_int32, C.c_uint32, C.c_float, _F32P]),
+    "xpbi_set_solver": (C.c_int, [_P, C.c_int32, C.c_float, C.c_int32, C.c_int32]),
+    "xpbi_set_network": (C.c_int, [_P, _F32P, C.c_uint32]),
+    "xpbi_read_residuals": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_int32)]),
+    "xpbi_read_training": (C.c_int, [_P, C.c_uint32, _F32P, _F32P, _F32P]),
 }
 
 

@@ -271,6 +271,14 @@ struct xpbi_sim {
   cudaGraphExec_t gexec = nullptr;
   std::string gkey;
   std::vector<void*> allocs;
+  // solver mode: 0 plain (reference), 1 network warm start, 2 previous-multiplier warm start
+  int mode = 0;
+  float residTol = 0.f;     // early stop tolerance relative to |C(v_pred)|; <= 0 off
+  bool track = false;       // residual history per iteration
+  bool features = false;    // compute network features every substep (training logs)
+  bool netLoaded = false;
+  float* netParams = nullptr;
+  int* netErr = nullptr;
 };
 
 namespace {
@@ -308,6 +316,7 @@ int upload(xpbi_sim* s) {
   s->matWordsHost.assign((size_t)S * kMaxMats * XPBI_MATERIAL_WORDS, 0u);
   for (uint32_t i = 0; i < S; ++i) {
     buildSceneDev(s->sc[i], i, s->sdev[i], &s->mdev[(size_t)i * kMaxMats]);
+    s->sdev[i].residTol = s->residTol;
     for (uint32_t m = 0; m < s->sc[i].nMats; ++m)
       packMaterial(s->sc[i].mats[m], s->sc[i].V0, &s->matWordsHost[((size_t)i * kMaxMats + m) * XPBI_MATERIAL_WORDS]);
   }
@@ -324,15 +333,27 @@ int upload(xpbi_sim* s) {
 struct Schedule {
   int K = 0;
   std::vector<char> pbf;
+  int mode = 0;          // 0 plain, 1 network warm start, 2 previous-multiplier warm start
+  bool track = false;    // residual history (includes the pass after the last iteration)
+  bool reduce = false;   // per-iteration residual reductions (history or early stop)
+  bool features = false; // network features at iteration 0
+  bool keepLam = false;  // carry the final multipliers into the next substep
   std::string key() const {
     std::string k = std::to_string(K) + ":";
     for (char c : pbf) k += c ? '1' : '0';
+    k += ":" + std::to_string(mode) + (track ? "t" : "") + (reduce ? "r" : "") + (features ? "f" : "") +
+         (keepLam ? "l" : "");
     return k;
   }
 };
 
 Schedule schedule(const xpbi_sim* s) {
   Schedule sch;
+  sch.mode = s->mode;
+  sch.track = s->track;
+  sch.reduce = s->track || s->residTol > 0.f;
+  sch.features = s->features || s->mode == 1;
+  sch.keepLam = s->mode != 0 || sch.features;
   for (const SceneHost& h : s->sc) sch.K = std::max(sch.K, h.iterations);
   sch.pbf.assign(sch.K, 0);
   for (const SceneHost& h : s->sc) {
@@ -371,14 +392,36 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
   R.mark(st, "scan");
   launch_scatter(b, st);
   R.mark(st, "fill");
-  launch_reorder(b, st);
+  launch_reorder(b, sch.keepLam, st);
   R.mark(st, "reorder");
   launch_computeL(b, st);
   R.mark(st, "computeL");
+  if (sch.features) {
+    launch_features(b, b.velS[0], st);
+    R.mark(st, "features");
+  }
+  if (sch.mode == 1) {
+    mlp_forward(b.feat, b.N, b.netBlob, b.netOut, nullptr, s->netErr, st);
+    R.mark(st, "network");
+    launch_warm_from_net(b, st);
+    R.mark(st, "warmstart");
+  } else if (sch.mode == 2) {
+    launch_warm_from_prev(b, st);
+    R.mark(st, "warmstart");
+  }
+  if (sch.reduce) {
+    cudaMemsetAsync(b.done, 0, sizeof(int) * b.S, st);
+    cudaMemsetAsync(b.itersUsed, 0, sizeof(int) * b.S, st);
+  }
+  const int aflags = (sch.reduce ? kTrackResid : 0) | (sch.mode != 0 ? kWarm : 0);
   int in = 0;
   for (int k = 0; k < sch.K; ++k) {
-    launch_solveA(b, k, b.velS[in], st);
+    launch_solveA(b, k, b.velS[in], aflags, st);
     R.mark(st, "solveA");
+    if (sch.reduce) {
+      launch_resid_reduce(b, k, st);
+      R.mark(st, "residual");
+    }
     launch_solveB(b, k, b.velS[in], b.velS[in ^ 1], sch.pbf[k] != 0, st);
     R.mark(st, "solveB");
     in ^= 1;
@@ -390,16 +433,31 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
       in ^= 1;
     }
   }
+  if (sch.track) {  // residual of the state the iterations leave behind
+    launch_solveA(b, sch.K, b.velS[in], kTrackResid | kMeasureOnly, st);
+    R.mark(st, "solveA(measure)");
+    launch_resid_reduce(b, -1, st);
+    R.mark(st, "residual");
+  }
   launch_xsph(b, b.velS[in], b.velS[in ^ 1], st);
   R.mark(st, "xsph");
   in ^= 1;
   launch_updateF_integrate(b, b.velS[in], st);
   R.mark(st, "updateF+integrate");
+  if (sch.keepLam) {
+    launch_keep_lambda(b, st);
+    R.mark(st, "keepLambda");
+  }
 }
 
 int kernelsPerSubstep(const Schedule& sch) {
   int n = 5 /* count, scan, fill, bigcells, reorder */ + 1 /* computeL */ + 2 /* xsph, updateF+integrate */;
-  for (int k = 0; k < sch.K; ++k) n += 2 + (sch.pbf[k] ? 2 : 0);
+  for (int k = 0; k < sch.K; ++k) n += 2 + (sch.pbf[k] ? 2 : 0) + (sch.reduce ? 2 : 0);
+  if (sch.features) n += 1;
+  if (sch.mode == 1) n += 2;
+  if (sch.mode == 2) n += 1;
+  if (sch.track) n += 3;
+  if (sch.keepLam) n += 1;
   return n;
 }
 
@@ -480,6 +538,25 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   A(b.nbrP, (size_t)kNbrCap * n);
   A(b.nbrPCount, n);
   A(b.xc, n);
+  A(b.lamOut, n);
+  A(b.lamPrev, n);
+  A(b.lamWarm, n);
+  A(b.feat, (size_t)kFeat * n);
+  A(b.netOut, n);
+  A(b.rr, n);
+  A(b.c0sq, n);
+  A(b.residPart, (size_t)nScenes * kResidChunks * 2);
+  A(b.resid, (size_t)nScenes * kMaxResid);
+  A(b.c0, nScenes);
+  A(b.done, nScenes);
+  A(b.itersUsed, nScenes);
+  {
+    uint8_t* blob = nullptr;
+    A(blob, mlp_blob_bytes());
+    b.netBlob = blob;
+  }
+  A(s->netParams, 9473);
+  A(s->netErr, 1);
   A(b.scenes, nScenes);
   A(b.mats, (size_t)nScenes * kMaxMats);
   A(b.err, 1);
@@ -515,9 +592,17 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
             H2D(b.state, state.data(), 4 * n) && H2D(b.lam, zero.data(), 4 * n) &&
             H2D(b.pbfLam, zero.data(), 4 * n) && H2D(b.sceneOf, sceneOf.data(), 2 * n) &&
             cudaMemset(b.err, 0, sizeof(int)) == cudaSuccess && cudaMemset(b.L, 0, 36 * n) == cudaSuccess &&
-            cudaMemset(b.sortedIdx, 0, 4 * n) == cudaSuccess &&
+            cudaMemset(b.sortedIdx, 0, 4 * n) == cudaSuccess && cudaMemset(b.lamOut, 0, 4 * n) == cudaSuccess &&
+            cudaMemset(b.lamPrev, 0, 4 * n) == cudaSuccess && cudaMemset(b.lamWarm, 0, 4 * n) == cudaSuccess &&
+            cudaMemset(b.done, 0, sizeof(int) * nScenes) == cudaSuccess &&
+            cudaMemset(b.itersUsed, 0, sizeof(int) * nScenes) == cudaSuccess &&
+            cudaMemset(b.resid, 0, sizeof(double) * nScenes * kMaxResid) == cudaSuccess &&
+            cudaMemset(s->netErr, 0, sizeof(int)) == cudaSuccess &&
             cudaMemset(b.cellStart, 0, 4 * ((size_t)b.C + 4)) == cudaSuccess;
   if (!ok) return bail(fail(XPBI_ERR_CUDA, "initial upload failed"));
+  // sets the network kernel's shared-memory attribute outside any capture
+  if (mlp_forward(nullptr, 0, nullptr, nullptr, nullptr, nullptr, s->stream) != cudaSuccess)
+    return bail(fail(XPBI_ERR_CUDA, "network kernel attribute"));
   rc = upload(s);
   if (rc != XPBI_OK) return bail(rc);
   if (cudaStreamSynchronize(s->stream) != cudaSuccess) return bail(fail(XPBI_ERR_CUDA, "initial sync failed"));
@@ -543,11 +628,14 @@ int applySchedule(xpbi_sim* s, int32_t iterations, int32_t hasWater) {
 }
 
 int checkDeviceErr(xpbi_sim* s) {
-  int e = 0;
+  int e = 0, en = 0;
   XPBI_CK(cudaMemcpyAsync(&e, s->b.err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  XPBI_CK(cudaMemcpyAsync(&en, s->netErr, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
   XPBI_CK(cudaStreamSynchronize(s->stream));
+  e |= en;
   if (e) {
     cudaMemsetAsync(s->b.err, 0, sizeof(int), s->stream);
+    cudaMemsetAsync(s->netErr, 0, sizeof(int), s->stream);
     cudaStreamSynchronize(s->stream);
     char msg[96];
     std::snprintf(msg, sizeof(msg), "device error word 0x%x (bounded wait expired in the prefix scan)", e);
@@ -801,6 +889,7 @@ int xpbi_write_state(xpbi_sim* sim, uint32_t scene, const float* pos4, const flo
       pl[i] = aux4[4 * i + 3];
     }
     XPBI_CK(cudaMemcpy(b.lam + o, lam.data(), 4 * n, cudaMemcpyHostToDevice));
+    XPBI_CK(cudaMemcpy(b.lamOut + o, lam.data(), 4 * n, cudaMemcpyHostToDevice));  // warm starts from it
     XPBI_CK(cudaMemcpy(b.state + o, st.data(), 4 * n, cudaMemcpyHostToDevice));
     XPBI_CK(cudaMemcpy(b.pbfLam + o, pl.data(), 4 * n, cudaMemcpyHostToDevice));
   }
@@ -876,6 +965,71 @@ int xpbi_device_ptrs(xpbi_sim* sim, void** pos4, void** vel4, void** materials) 
   if (pos4) *pos4 = sim->b.pos;
   if (vel4) *vel4 = sim->b.vel;
   if (materials) *materials = sim->matWords;
+  return XPBI_OK;
+}
+
+int xpbi_set_solver(xpbi_sim* sim, int32_t mode, float rel_tol, int32_t track_residual, int32_t log_features) {
+  XPBI_TRY(checkSim(sim));
+  if (mode < 0 || mode > 2) return fail(XPBI_ERR_INVALID, "solver mode must be 0, 1 or 2");
+  if (mode == 1 && !sim->netLoaded) return fail(XPBI_ERR_INVALID, "network warm start needs xpbi_set_network first");
+  if (!(rel_tol <= 1.f) || !std::isfinite(rel_tol)) return fail(XPBI_ERR_INVALID, "rel_tol must be <= 1");
+  sim->mode = mode;
+  sim->residTol = rel_tol;
+  sim->track = track_residual != 0;
+  sim->features = log_features != 0;
+  sim->dirty = true;
+  return XPBI_OK;
+}
+
+int xpbi_set_network(xpbi_sim* sim, const float* params, uint32_t count) {
+  XPBI_TRY(checkSim(sim));
+  if (!params || count != 9473u) return fail(XPBI_ERR_INVALID, "network needs 9473 parameters");
+  XPBI_CK(cudaMemcpyAsync(sim->netParams, params, sizeof(float) * count, cudaMemcpyHostToDevice, sim->stream));
+  mlp_pack(sim->netParams, sim->b.netBlob, sim->stream);
+  XPBI_CK(cudaGetLastError());
+  XPBI_CK(cudaStreamSynchronize(sim->stream));
+  sim->netLoaded = true;
+  return XPBI_OK;
+}
+
+int xpbi_read_residuals(xpbi_sim* sim, uint32_t scene, double* norms, int32_t cap, int32_t* iterations_run) {
+  XPBI_TRY(checkSim(sim));
+  if (scene >= sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
+  XPBI_TRY(xpbi_synchronize(sim));
+  std::vector<double> r(kMaxResid);
+  double c0 = 0;
+  int used = 0;
+  XPBI_CK(cudaMemcpy(r.data(), sim->b.resid + (size_t)scene * kMaxResid, sizeof(double) * kMaxResid,
+                     cudaMemcpyDeviceToHost));
+  XPBI_CK(cudaMemcpy(&c0, sim->b.c0 + scene, sizeof(double), cudaMemcpyDeviceToHost));
+  XPBI_CK(cudaMemcpy(&used, sim->b.itersUsed + scene, sizeof(int), cudaMemcpyDeviceToHost));
+  const int K = sim->sc[scene].iterations;
+  if (iterations_run) *iterations_run = used;
+  if (norms && cap > 0) {
+    // [ |C(v_pred)|, |r_0| .. |r_{K-1}|, |r| after the last applied iteration ]
+    std::vector<double> out;
+    out.push_back(std::sqrt(c0));
+    for (int k = 0; k < K && k < kMaxResid - 1; ++k) out.push_back(k < used + 1 ? std::sqrt(r[k]) : NAN);
+    out.push_back(std::sqrt(r[kMaxResid - 1]));
+    for (int q = 0; q < cap && q < (int)out.size(); ++q) norms[q] = out[q];
+  }
+  return XPBI_OK;
+}
+
+int xpbi_read_training(xpbi_sim* sim, uint32_t scene, float* features16, float* target, float* alpha_tilde) {
+  XPBI_TRY(checkSim(sim));
+  if (scene >= sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
+  XPBI_TRY(xpbi_synchronize(sim));
+  const SceneHost& h = sim->sc[scene];
+  const size_t n = h.n, o = h.pBase;
+  if (features16) XPBI_CK(cudaMemcpy(features16, sim->b.feat + o * kFeat, sizeof(float) * kFeat * n,
+                                      cudaMemcpyDeviceToHost));
+  const float aT = sim->sdev[scene].alphaT;
+  if (target) {
+    XPBI_CK(cudaMemcpy(target, sim->b.lam + o, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; ++i) target[i] *= aT;
+  }
+  if (alpha_tilde) *alpha_tilde = aT;
   return XPBI_OK;
 }
 

@@ -240,25 +240,28 @@ __device__ __forceinline__ M3 velocityGradient(const Bufs& b, const Ctx& cx, uin
 //   sgrad = -M s,  denom = <M^T M, Q> + |sgrad|^2 / m_i,  cdot = <M, grad v>.
 // (The last identity also removes the cancellation of the reference's
 // sum_b g_b . v_b against sgrad . v_i when the body moves as a whole.)
-__global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4* __restrict__ velIn) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= b.N) return;
-  const Ctx cx = ctxOf(b, i);
+// Constraint of a solid slot at the current velocities: the single sweep
+// above plus the trial F, SVD, return map and the closed-form sums.
+struct Constraint {
+  float C;        // sqrt(2 Psi) at the projected state (0 below 1e-7)
+  float denom;    // sum |grad C|^2 / m, self term included
+  float cdot;     // grad C . v
+  M3 GL;          // (dC/dF) F^nT L
+  V3 sgrad;       // self gradient (per unit multiplier)
+  V3 logSigTr;    // log of the trial singular values (clamped like safeSig)
+  float nNbr;     // solid neighbours in the sweep
+};
+
+__device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& cx, uint32_t i, float4 pi,
+                                                     const float4* __restrict__ velIn, const MatDev& m, float st) {
   const SceneDev& S = *cx.scene;
-  if (k >= S.iterations) return;
   const float4* __restrict__ posS = b.posS;
-  const float4 pi = posS[i];
-  if (waterW(pi.w)) return;  // water: Sp is never read
-  const uint32_t mi = matOfW(pi.w);
-  const float st = b.stateS[i];
-  const MatDev m = hardenedMat(cx.mats[mi], st);
   const V3 xi = xyz(pi);
-  const float4 vi4 = velIn[i];
-  const V3 vi = xyz(vi4);
+  const V3 vi = xyz(velIn[i]);
   const M3 Li = loadM(b.L, b.N, i);
   M3 G = mzero();
   V3 sv = splat(0.f);
-  float q00 = 0.f, q11 = 0.f, q22 = 0.f, q01 = 0.f, q02 = 0.f, q12 = 0.f;
+  float q00 = 0.f, q11 = 0.f, q22 = 0.f, q01 = 0.f, q02 = 0.f, q12 = 0.f, cnt = 0.f;
   forNbrs(b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
           [&](uint32_t, bool water, const PV& d) {
             if (water) return;
@@ -275,34 +278,224 @@ __global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4
             q01 += cg.x * gt.y;
             q02 += cg.x * gt.z;
             q12 += cg.y * gt.z;
+            cnt += 1.f;
           });
+  Constraint out;
+  out.nNbr = cnt;
   const M3 Fn = loadM(b.FS, b.N, i);
   const M3 Ftr = mul(madd(mident(), mscale(G, S.dt)), Fn);
   const SVD sd = svd3Fast(Ftr);
+  out.logSigTr = vlog(safeSig(sd.sig));
   float stOut;
   const V3 sig = returnMap(sd.sig, m, st, S.dt, stOut);
   const float psi = stvkPsi(sig, m.mu, m.lam);
-  const float C = sqrtf(fmaxf(2.f * psi, 0.f));
-  if (C < 1e-7f) {
-    storeSp(b.Sp, i, mzero(), splat(0.f));
-    return;
+  out.C = sqrtf(fmaxf(2.f * psi, 0.f));
+  if (out.C < 1e-7f) {
+    out.C = 0.f;
+    out.denom = 0.f;
+    out.cdot = 0.f;
+    out.GL = mzero();
+    out.sgrad = splat(0.f);
+    return out;
   }
   const V3 dpsi = stvkDPsi(sig, m.mu, m.lam);
-  const M3 Pk = diagMul(sd.U, dpsi * __frcp_rn(C), sd.V);
+  const M3 Pk = diagMul(sd.U, dpsi * __frcp_rn(out.C), sd.V);
   const M3 Mm = mul(Pk, transpose(Fn));
-  const M3 GL = mul(Mm, Li);
-  const V3 sgrad = -mul(Mm, sv);
+  out.GL = mul(Mm, Li);
+  out.sgrad = -mul(Mm, sv);
   // <M^T M, Q> = sum over column pairs (a, b) of (M_a . M_b) Q_ab
   const V3 c0 = Mm.c[0], c1 = Mm.c[1], c2 = Mm.c[2];
   const float denomN = dot(c0, c0) * q00 + dot(c1, c1) * q11 + dot(c2, c2) * q22 +
                        2.f * (dot(c0, c1) * q01 + dot(c0, c2) * q02 + dot(c1, c2) * q12);
-  const float denom = denomN + dot(sgrad, sgrad) / m.mass;
-  const float cdot = dot(Mm.c[0], G.c[0]) + dot(Mm.c[1], G.c[1]) + dot(Mm.c[2], G.c[2]);
+  out.denom = denomN + dot(out.sgrad, out.sgrad) / m.mass;
+  out.cdot = dot(Mm.c[0], G.c[0]) + dot(Mm.c[1], G.c[1]) + dot(Mm.c[2], G.c[2]);
+  return out;
+}
+
+__device__ __forceinline__ bool sceneDone(const Bufs& b, uint32_t i) {
+  const uint32_t s = b.S > 1 ? (uint32_t)b.sceneOf[i] : 0u;
+  return b.done[s] != 0;
+}
+
+// Inelastic constraint pass A (simkernels.js:248-309).
+//
+// flags & kTrackResid: writes the XPBD residual r = C + alphaT lambda of the
+//   state entering this iteration (damping excluded) to rr, and C^2 to c0sq
+//   at iteration 0.
+// flags & kWarm (iteration 0): starts from lambda0 = lamWarm instead of 0.
+//   Its impulse has not been applied to the velocities this pass sees, so the
+//   first correction uses the linearised post-impulse constraint
+//   C + denom lambda0 (the particle's own response, the Jacobi diagonal):
+//     dlam = omega (-C - (denom + alphaT) lambda0 - gamma dt cdot) / ((1+gamma) denom + alphaT)
+//   and the applied impulse is lambda0 + dlam. A warm value that would not
+//   reduce the particle's own residual, |C + (denom + alphaT) lambda0| >= C,
+//   is replaced by the plain start lambda0 = 0. With lambda0 = 0 both
+//   updates are the reference's.
+// flags & kMeasureOnly: residual only (the pass after the last iteration).
+__global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4* __restrict__ velIn, int flags) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.N) return;
+  const Ctx cx = ctxOf(b, i);
+  const SceneDev& S = *cx.scene;
+  const bool track = (flags & kTrackResid) != 0;
+  const bool measure = (flags & kMeasureOnly) != 0;
+  const bool warm0 = (flags & kWarm) != 0 && k == 0;
+  const float4 pi = b.posS[i];
+  const bool active = measure || (k < S.iterations && !sceneDone(b, i));
+  if (!active || waterW(pi.w)) {  // water: Sp is never read
+    if (track) {
+      b.rr[i] = 0.f;
+      if (k == 0) b.c0sq[i] = 0.f;
+    }
+    return;
+  }
+  const uint32_t mi = matOfW(pi.w);
+  const float st = b.stateS[i];
+  const MatDev m = hardenedMat(cx.mats[mi], st);
+  const Constraint c = evalConstraint(b, cx, i, pi, velIn, m, st);
+  float lam0 = k == 0 ? (warm0 ? b.lamWarm[i] : 0.f) : b.lam[i];
+  if (warm0 && !(fabsf(c.C + (c.denom + S.alphaT) * lam0) < c.C)) lam0 = 0.f;
+  if (track) {
+    const float r = warm0 ? c.C + (c.denom + S.alphaT) * lam0 : c.C + S.alphaT * lam0;
+    b.rr[i] = r * r;
+    if (k == 0) b.c0sq[i] = c.C * c.C;
+  }
+  if (measure) return;
+  if (c.C == 0.f) {
+    if (k == 0) b.lam[i] = lam0;
+    storeSp(b.Sp, i, mzero(), splat(0.f));
+    return;
+  }
   const float g = S.kDamp;
-  const float lam0 = b.lam[i];
-  const float dlam = S.omega * (-C - S.alphaT * lam0 - g * S.dt * cdot) / ((1.f + g) * denom + S.alphaT);
+  const float lamTerm = warm0 ? (c.denom + S.alphaT) * lam0 : S.alphaT * lam0;
+  const float dlam = S.omega * (-c.C - lamTerm - g * S.dt * c.cdot) / ((1.f + g) * c.denom + S.alphaT);
   b.lam[i] = lam0 + dlam;
-  storeSp(b.Sp, i, mscale(GL, dlam), sgrad * dlam);
+  const float imp = warm0 ? lam0 + dlam : dlam;
+  storeSp(b.Sp, i, mscale(c.GL, imp), c.sgrad * imp);
+}
+
+// Network features of every slot at iteration 0 (zeros for water):
+//   0-2  log singular values of the trial F
+//   3    C = sqrt(2 Psi) at the projected trial state
+//   4    alphaT * lambda of the previous substep (same particle)
+//   5    alphaT * lambda_1, lambda_1 = -C / (denom + alphaT): the particle's
+//        own Newton step, blind to its neighbours
+//   6    log10(1 + denom / alphaT): stiffness of the constraint vs compliance
+//   7    solid neighbours / 32
+//   8-14 material kind one-hot
+//   15   log10(mu) - 4.5
+__global__ void __launch_bounds__(kThreads) k_features(Bufs b, const float4* __restrict__ velIn) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.N) return;
+  const Ctx cx = ctxOf(b, i);
+  const SceneDev& S = *cx.scene;
+  const float4 pi = b.posS[i];
+  float f[kFeat];
+#pragma unroll
+  for (int q = 0; q < kFeat; ++q) f[q] = 0.f;
+  if (!waterW(pi.w) && S.iterations > 0) {
+    const uint32_t mi = matOfW(pi.w);
+    const float st = b.stateS[i];
+    const MatDev m = hardenedMat(cx.mats[mi], st);
+    const Constraint c = evalConstraint(b, cx, i, pi, velIn, m, st);
+    const float aT = S.alphaT;
+    f[0] = c.logSigTr.x;
+    f[1] = c.logSigTr.y;
+    f[2] = c.logSigTr.z;
+    f[3] = c.C;
+    f[4] = aT * b.lamPrev[i];
+    f[5] = -c.C * aT / (c.denom + aT);
+    f[6] = log10f(1.f + c.denom / aT);
+    f[7] = c.nNbr * (1.f / 32.f);
+    const uint32_t kind = cx.mats[mi].kind;
+    if (kind < 7u) f[8 + kind] = 1.f;
+    f[15] = log10f(fmaxf(m.mu, 1e-6f)) - 4.5f;
+  }
+  float4* out = reinterpret_cast<float4*>(b.feat + (size_t)i * kFeat);
+#pragma unroll
+  for (int q = 0; q < kFeat / 4; ++q) out[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+}
+
+// lambda_warm = network output / alphaT (the network predicts alphaT lambda)
+__global__ void k_warm_from_net(Bufs b) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.N) return;
+  const Ctx cx = ctxOf(b, i);
+  const float4 pi = b.posS[i];
+  b.lamWarm[i] = waterW(pi.w) ? 0.f : b.netOut[i] / cx.scene->alphaT;
+}
+
+// warm start from the previous substep's multiplier alone (no network)
+__global__ void k_warm_from_prev(Bufs b) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.N) return;
+  b.lamWarm[i] = b.lamPrev[i];
+}
+
+// Per-scene residual norms, deterministic: block (c, s) sums chunk c of
+// scene s in a fixed order; k_resid_final adds the chunks in order.
+__global__ void __launch_bounds__(256) k_resid_partial(Bufs b, int k) {
+  __shared__ double red[2][256];
+  const uint32_t s = blockIdx.y, c = blockIdx.x;
+  const SceneDev& S = b.scenes[s];
+  const uint32_t n = S.n, base = S.pBase;
+  const uint32_t lo = base + (uint32_t)(((uint64_t)n * c) / kResidChunks);
+  const uint32_t hi = base + (uint32_t)(((uint64_t)n * (c + 1)) / kResidChunks);
+  double a = 0.0, a0 = 0.0;
+  if (!b.done[s] || k < 0) {
+    for (uint32_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+      a += (double)b.rr[p];
+      if (k == 0) a0 += (double)b.c0sq[p];
+    }
+  }
+  red[0][threadIdx.x] = a;
+  red[1][threadIdx.x] = a0;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + w];
+      red[1][threadIdx.x] += red[1][threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    b.residPart[(s * kResidChunks + c) * 2] = red[0][0];
+    b.residPart[(s * kResidChunks + c) * 2 + 1] = red[1][0];
+  }
+}
+
+// k >= 0: iteration k's residual (early stop); k < 0: after the last
+// iteration (slot kMaxResid - 1).
+__global__ void k_resid_final(Bufs b, int k) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= b.S) return;
+  const SceneDev& S = b.scenes[s];
+  if (k >= 0 && (b.done[s] || k >= S.iterations)) return;
+  double a = 0.0, a0 = 0.0;
+  for (int c = 0; c < kResidChunks; ++c) {
+    a += b.residPart[(s * kResidChunks + c) * 2];
+    a0 += b.residPart[(s * kResidChunks + c) * 2 + 1];
+  }
+  if (k < 0) {
+    b.resid[(size_t)s * kMaxResid + (kMaxResid - 1)] = a;
+    return;
+  }
+  if (k < kMaxResid - 1) b.resid[(size_t)s * kMaxResid + k] = a;
+  if (k == 0) b.c0[s] = a0;
+  const double tol = (double)S.residTol;
+  if (tol > 0.0 && a <= tol * tol * b.c0[s]) {
+    b.done[s] = 1;
+    b.itersUsed[s] = k;
+  } else {
+    b.itersUsed[s] = k + 1;
+  }
+}
+
+// keep this substep's final multipliers for the next substep's features
+__global__ void k_keep_lambda(Bufs b) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.N) return;
+  b.lamOut[i] = b.lam[i];
 }
 
 // applyBoundary (simkernels.js:369-404)
@@ -359,7 +552,7 @@ __global__ void __launch_bounds__(kThreads) k_solveB(Bufs b, int k, const float4
   const float4* __restrict__ Sp = b.Sp;
   const float4 vi4 = velIn[i];
   const float4 pi = posS[i];
-  if (k >= S.iterations) {
+  if (k >= S.iterations || sceneDone(b, i)) {
     velOut[i] = vi4;
     if (writeXc) {
       const V3 xc = xyz(pi) + S.dt * xyz(vi4);
@@ -623,9 +816,19 @@ inline unsigned grid(uint32_t n) { return (unsigned)((n + kThreads - 1) / kThrea
 }  // namespace
 
 void launch_computeL(const Bufs& b, cudaStream_t st) { k_computeL<<<grid(b.N), kThreads, 0, st>>>(b); }
-void launch_solveA(const Bufs& b, int k, const float4* velIn, cudaStream_t st) {
-  k_solveA<<<grid(b.N), kThreads, 0, st>>>(b, k, velIn);
+void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, cudaStream_t st) {
+  k_solveA<<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, flags);
 }
+void launch_features(const Bufs& b, const float4* velIn, cudaStream_t st) {
+  k_features<<<grid(b.N), kThreads, 0, st>>>(b, velIn);
+}
+void launch_warm_from_net(const Bufs& b, cudaStream_t st) { k_warm_from_net<<<grid(b.N), kThreads, 0, st>>>(b); }
+void launch_warm_from_prev(const Bufs& b, cudaStream_t st) { k_warm_from_prev<<<grid(b.N), kThreads, 0, st>>>(b); }
+void launch_resid_reduce(const Bufs& b, int k, cudaStream_t st) {
+  k_resid_partial<<<dim3(kResidChunks, b.S), 256, 0, st>>>(b, k);
+  k_resid_final<<<(b.S + 127) / 128, 128, 0, st>>>(b, k);
+}
+void launch_keep_lambda(const Bufs& b, cudaStream_t st) { k_keep_lambda<<<grid(b.N), kThreads, 0, st>>>(b); }
 void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, cudaStream_t st) {
   k_solveB<<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, writeXc ? 1 : 0);
 }

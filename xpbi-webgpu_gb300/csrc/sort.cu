@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(kBigThreads) k_bigcells(Bufs b, uint32_t* scra
 
 // Final slot + physical reorder with the scatter pass's predictor fused in
 // (simkernels.js:137-146 and 154-186).
-__global__ void __launch_bounds__(kThreads) k_reorder(Bufs b) {
+__global__ void __launch_bounds__(kThreads) k_reorder(Bufs b, int keepLam) {
   uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= b.N) return;
   uint32_t i = b.tmp[p];
@@ -253,6 +253,7 @@ __global__ void __launch_bounds__(kThreads) k_reorder(Bufs b) {
   b.velS[0][s] = make_float4(vn.x, vn.y, vn.z, Vn);
   b.stateS[s] = b.state[i];
   b.lam[s] = 0.f;
+  if (keepLam) b.lamPrev[s] = b.lamOut[i];
 }
 
 inline unsigned grid(uint32_t n, int t) { return (unsigned)((n + t - 1) / t); }
@@ -275,12 +276,12 @@ void launch_scan(const Bufs& b, cudaStream_t st) {
 void launch_scatter(const Bufs& b, cudaStream_t st) {
   k_fill<<<grid(b.N, kThreads), kThreads, 0, st>>>(b);
 }
-void launch_reorder(const Bufs& b, cudaStream_t st) {
+void launch_reorder(const Bufs& b, bool keepLam, cudaStream_t st) {
   // scratch for buckets too large for shared memory lives in the Sp buffer
   // (12 floats per particle >= 2 words per particle), unused until solveA
   uint32_t* scratch = reinterpret_cast<uint32_t*>(b.Sp);
   k_bigcells<<<kBigGrid, kBigThreads, kSmemSortCap * sizeof(uint32_t), st>>>(b, scratch);
-  k_reorder<<<grid(b.N, kThreads), kThreads, 0, st>>>(b);
+  k_reorder<<<grid(b.N, kThreads), kThreads, 0, st>>>(b, keepLam ? 1 : 0);
 }
 
 }  // namespace xpbi

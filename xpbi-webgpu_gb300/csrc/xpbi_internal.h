@@ -11,6 +11,14 @@ constexpr uint32_t kKindSnow = 5u;
 constexpr uint32_t kKindWater = 6u;
 
 constexpr uint32_t kNbrCap = 64u;      // neighbour-list capacity per particle
+constexpr int kResidChunks = 16;       // per-scene partial sums of the residual
+constexpr int kMaxResid = 129;         // residual slots per scene (iterations + 1)
+constexpr int kFeat = 16;              // network features per particle
+
+// solveA flags
+constexpr int kTrackResid = 1;         // write per-particle residuals
+constexpr int kWarm = 2;               // iteration 0 starts from lamWarm
+constexpr int kMeasureOnly = 4;        // residual only: no multiplier / impulse update
 constexpr uint32_t kNbrOverflow = 0xffffffffu;
 constexpr uint32_t kWaterBit = 0x80000000u;
 
@@ -55,6 +63,7 @@ struct SceneDev {
   int iterations;           // XPBI Jacobi iterations this substep
   int pbfIterations;        // PBF passes (first k iterations)
   int hasWater;
+  float residTol;           // early stop at |r_k| <= residTol |C(v_pred)|; <= 0: never
 };
 
 struct MatDev {
@@ -97,6 +106,20 @@ struct Bufs {
   uint32_t* nbrP;       // [N][kNbrCap] predicted-position neighbours of the current PBF pass
   uint32_t* nbrPCount;  // [N]
   float4* xc;           // [N] predicted positions x + dt v of the current PBF pass, w = pos.w
+  // solver instrumentation and warm start
+  float* lamOut;        // [N] final multiplier of the last substep, current order
+  float* lamPrev;       // [N] the same, carried into this substep's sorted order
+  float* lamWarm;       // [N] warm-start multiplier for iteration 0 (sorted)
+  float* feat;          // [N][16] network features at iteration 0 (sorted)
+  float* netOut;        // [N] network output
+  float* rr;            // [N] squared constraint residual of the current iteration
+  float* c0sq;          // [N] squared constraint value at the predicted velocities
+  double* residPart;    // [S][kResidChunks] partial sums
+  double* resid;        // [S][kMaxResid] residual norm^2 per iteration (last slot: after the last)
+  double* c0;           // [S] |C(v_pred)|^2
+  int* done;            // [S] converged: later iterations skip
+  int* itersUsed;       // [S] iterations whose update was applied
+  void* netBlob;        // packed network weights
   SceneDev* scenes;     // [S]
   MatDev* mats;         // [S * 8]
   int* err;             // [1] device error word
@@ -108,12 +131,23 @@ struct Bufs {
 void launch_count(const Bufs& b, cudaStream_t st);
 void launch_scan(const Bufs& b, cudaStream_t st);
 void launch_scatter(const Bufs& b, cudaStream_t st);
-void launch_reorder(const Bufs& b, cudaStream_t st);
+void launch_reorder(const Bufs& b, bool keepLam, cudaStream_t st);
+void launch_warm_from_prev(const Bufs& b, cudaStream_t st);
 uint32_t scan_tiles(uint32_t cells);
 
 // ---- launchers (solve.cu) ----
 void launch_computeL(const Bufs& b, cudaStream_t st);
-void launch_solveA(const Bufs& b, int k, const float4* velIn, cudaStream_t st);
+void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, cudaStream_t st);
+void launch_features(const Bufs& b, const float4* velIn, cudaStream_t st);
+void launch_warm_from_net(const Bufs& b, cudaStream_t st);
+void launch_resid_reduce(const Bufs& b, int k, cudaStream_t st);
+void launch_keep_lambda(const Bufs& b, cudaStream_t st);
+
+// ---- network (mlp.cu) ----
+size_t mlp_blob_bytes();
+void mlp_pack(const float* dParams, void* dBlob, cudaStream_t st);
+cudaError_t mlp_forward(const float* dX, uint32_t rows, const void* dBlob, float* dY, float* dZ, int* dErr,
+                        cudaStream_t st);
 void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, cudaStream_t st);
 void launch_pbfA(const Bufs& b, int k, const float4* velIn, cudaStream_t st);
 void launch_pbfB(const Bufs& b, int k, const float4* velIn, float4* velOut, cudaStream_t st);

@@ -237,6 +237,37 @@ class Simulation:
         check(lib().xpbi_read_uniforms(self._h, scene, _uptr(pw), _uptr(mw)))
         return pw, mw
 
+    # -- solver modes and the warm-start network (not in the reference)
+    PLAIN, NETWORK, PREVIOUS = 0, 1, 2
+
+    def set_solver(self, mode: int = 0, rel_tol: float = 0.0, track_residual: bool = False,
+                   log_features: bool = False):
+        check(lib().xpbi_set_solver(self._h, mode, rel_tol, 1 if track_residual else 0, 1 if log_features else 0))
+
+    def set_network(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        check(lib().xpbi_set_network(self._h, _fptr(p), len(p)))
+
+    def read_residuals(self, scene: int = 0):
+        """(norms, iterations run): norms[0] = |C(v_pred)|, norms[1+k] =
+        |r_k|, norms[-1] = residual of the final state."""
+        it = self.scenes[scene]["iterations"] if "iterations" in self.scenes[scene] else 0
+        cap = 256
+        out = np.full(cap, np.nan)
+        used = C.c_int32()
+        check(lib().xpbi_read_residuals(self._h, scene, out.ctypes.data_as(C.POINTER(C.c_double)), cap,
+                                        C.byref(used)))
+        del it
+        return out, used.value
+
+    def read_training(self, scene: int = 0):
+        n = self.scene_sizes[scene]
+        f = np.empty((n, 16), np.float32)
+        t = np.empty(n, np.float32)
+        a = np.zeros(1, np.float32)
+        check(lib().xpbi_read_training(self._h, scene, _fptr(f), _fptr(t), _fptr(a)))
+        return f, t, float(a[0])
+
     def device_ptrs(self):
         p, v, m = C.c_void_p(), C.c_void_p(), C.c_void_p()
         check(lib().xpbi_device_ptrs(self._h, C.byref(p), C.byref(v), C.byref(m)))
