@@ -319,18 +319,22 @@ __device__ __forceinline__ bool sceneDone(const Bufs& b, uint32_t i) {
 
 // Inelastic constraint pass A (simkernels.js:248-309).
 //
-// flags & kTrackResid: writes the XPBD residual r = C + alphaT lambda of the
-//   state entering this iteration (damping excluded) to rr, and C^2 to c0sq
-//   at iteration 0.
+// flags & kTrackResid: writes r^2 for the residual of the state entering
+//   this iteration, r = C + alphaT lambda + gamma dt cdot (the numerator the
+//   damped update drives to zero; without the damping term the Jacobi fixed
+//   point sits at C + alphaT lambda = -gamma dt cdot, not 0), and at
+//   iteration 0 the residual at lambda = 0 to c0sq.
 // flags & kWarm (iteration 0): starts from lambda0 = lamWarm instead of 0.
 //   Its impulse has not been applied to the velocities this pass sees, so the
-//   first correction uses the linearised post-impulse constraint
-//   C + denom lambda0 (the particle's own response, the Jacobi diagonal):
-//     dlam = omega (-C - (denom + alphaT) lambda0 - gamma dt cdot) / ((1+gamma) denom + alphaT)
+//   first correction uses the linearised post-impulse residual: applying
+//   lambda0 moves C by denom lambda0 and gamma dt cdot by gamma denom lambda0
+//   (the particle's own response, the Jacobi diagonal), so
+//     r = C + gamma dt cdot + ((1+gamma) denom + alphaT) lambda0,
+//     dlam = -omega r / ((1+gamma) denom + alphaT),
 //   and the applied impulse is lambda0 + dlam. A warm value that would not
-//   reduce the particle's own residual, |C + (denom + alphaT) lambda0| >= C,
-//   is replaced by the plain start lambda0 = 0. With lambda0 = 0 both
-//   updates are the reference's.
+//   reduce the particle's own residual, |r| >= |C + gamma dt cdot|, is
+//   replaced by the plain start lambda0 = 0 (the plain solve stays the
+//   fallback). With lambda0 = 0 both updates are the reference's.
 // flags & kMeasureOnly: residual only (the pass after the last iteration).
 __global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4* __restrict__ velIn, int flags) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -353,12 +357,17 @@ __global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4
   const float st = b.stateS[i];
   const MatDev m = hardenedMat(cx.mats[mi], st);
   const Constraint c = evalConstraint(b, cx, i, pi, velIn, m, st);
+  const float g = S.kDamp;
+  const float stiff = (1.f + g) * c.denom + S.alphaT;  // d(residual) / d(applied multiplier)
+  const float r0 = c.C + g * S.dt * c.cdot;            // residual at lambda = 0
   float lam0 = k == 0 ? (warm0 ? b.lamWarm[i] : 0.f) : b.lam[i];
-  if (warm0 && !(fabsf(c.C + (c.denom + S.alphaT) * lam0) < c.C)) lam0 = 0.f;
+  if (warm0 && !(fabsf(r0 + stiff * lam0) < fabsf(r0))) lam0 = 0.f;
+  // the quantity the update drives to zero: r = C + alphaT lambda + gamma dt cdot
+  const float lamTerm = warm0 ? stiff * lam0 : S.alphaT * lam0;
   if (track) {
-    const float r = warm0 ? c.C + (c.denom + S.alphaT) * lam0 : c.C + S.alphaT * lam0;
+    const float r = r0 + lamTerm;
     b.rr[i] = r * r;
-    if (k == 0) b.c0sq[i] = c.C * c.C;
+    if (k == 0) b.c0sq[i] = r0 * r0;
   }
   if (measure) return;
   if (c.C == 0.f) {
@@ -366,9 +375,7 @@ __global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4
     storeSp(b.Sp, i, mzero(), splat(0.f));
     return;
   }
-  const float g = S.kDamp;
-  const float lamTerm = warm0 ? (c.denom + S.alphaT) * lam0 : S.alphaT * lam0;
-  const float dlam = S.omega * (-c.C - lamTerm - g * S.dt * c.cdot) / ((1.f + g) * c.denom + S.alphaT);
+  const float dlam = S.omega * (-c.C - lamTerm - g * S.dt * c.cdot) / stiff;
   b.lam[i] = lam0 + dlam;
   const float imp = warm0 ? lam0 + dlam : dlam;
   storeSp(b.Sp, i, mscale(c.GL, imp), c.sgrad * imp);
