@@ -160,6 +160,56 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line))
 
 
+def make_sim(xp, scenes, stream, preroll: int):
+    """A handle over the workload, rolled forward `preroll` plain substeps
+    (deterministic: equal inputs give equal states)."""
+    sim = xp.Simulation(scenes if len(scenes) > 1 else scenes[0])
+    sim.set_stream(stream.cuda_stream)
+    has_water = any(s["hasWater"] for s in scenes)
+    for k, s in enumerate(scenes):
+        sim.write_params(xp.params_for(s), scene=k)
+        sim.set_schedule(k, s["iterations"], s["hasWater"])
+    if preroll:
+        sim.set_solver(0, 0.0, False, True)  # carries multipliers for the warm start
+        sim.step(preroll, -1, has_water)
+    sim.synchronize()
+    return sim, has_water
+
+
+def timed_steps(sim, has_water, steps, stream, dist):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    sim.step(steps, -1, has_water)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    sim.synchronize()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms
+
+
+def residual_stats(sim, has_water, n_scenes, substeps):
+    """Final residual relative to the plain start, and iterations applied,
+    over `substeps` tracked substeps of every scene."""
+    rel, used = [], []
+    for _ in range(substeps):
+        sim.step(1, -1, has_water)
+        for k in range(n_scenes):
+            r, u = sim.read_residuals(k)
+            if r[0] > 0:
+                fin = r[1 + sim.scenes[k]["iterations"]]
+                rel.append(float(fin / r[0]))
+            used.append(u)
+    return rel, used
+
+
 def run_xpbi(args, rank: int, world: int):
     import torch
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -171,37 +221,50 @@ def run_xpbi(args, rank: int, world: int):
     xp, scenes = workload(args.workload, rank)
     n_total = sum(len(s["positions"]) for s in scenes)
     stream = torch.cuda.Stream()
-    sim = xp.Simulation(scenes if len(scenes) > 1 else scenes[0])
-    sim.set_stream(stream.cuda_stream)
-    has_water = any(s["hasWater"] for s in scenes)
-    for k, s in enumerate(scenes):
-        sim.write_params(xp.params_for(s), scene=k)
-        sim.set_schedule(k, s["iterations"], s["hasWater"])
-    launches = sim.launches_per_substep(-1, has_water)
+    learned = args.solver == "learned"
 
-    # warm-up (graph capture happens here)
-    sim.step(args.warmup, -1, has_water)
+    # ---- plain solve (the reference's fixed iteration budget)
+    sim, has_water = make_sim(xp, scenes, stream, args.preroll)
+    sim.set_solver(0, 0.0, False, False)
+    sim.step(args.warmup, -1, has_water)  # graph capture happens here
     sim.synchronize()
-
-    # ---- device-resident throughput: K graph replays, events on the launching stream
     clocks = Clocks(local)
     clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    e0.record(stream)
-    sim.step(args.steps, -1, has_water)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+    ms_plain = timed_steps(sim, has_water, args.steps, stream, dist)
     clk = clocks.stop()
-    sim.synchronize()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = n_total * world * args.steps / (ms / 1e3)
+    value_plain = n_total * world * args.steps / (ms_plain / 1e3)
+    launches = sim.launches_per_substep(-1, has_water)
+    solvers = {"plain": {"value": value_plain, "ms_per_step": ms_plain / args.steps,
+                         "iterations": [s["iterations"] for s in scenes][:4]}}
+    ms, value = ms_plain, value_plain
+    if learned:
+        # equal residual: the plain solve's own final residual, relative to
+        # its starting residual, median over tracked substeps and scenes
+        sim.set_solver(0, 0.0, True, True)
+        rel, _ = residual_stats(sim, has_water, len(scenes), args.residual_substeps)
+        tau = float(np.median(rel))
+        sim.close()
+        tw = importlib.import_module("xpbi-webgpu_gb300.train_warm")
+        net = tw.load_weights()
+        sim, has_water = make_sim(xp, scenes, stream, args.preroll)
+        sim.set_network(net)
+        sim.set_solver(1, tau, False, False)
+        sim.step(args.warmup, -1, has_water)
+        sim.synchronize()
+        clocks = Clocks(local)
+        clocks.start()
+        ms = timed_steps(sim, has_water, args.steps, stream, dist)
+        clk = clocks.stop()
+        value = n_total * world * args.steps / (ms / 1e3)
+        launches = sim.launches_per_substep(-1, has_water)
+        sim.set_solver(1, tau, True, False)
+        rel_l, used_l = residual_stats(sim, has_water, len(scenes), args.residual_substeps)
+        sim.set_solver(1, tau, False, False)
+        solvers["plain"]["final_rel_residual_median"] = tau
+        solvers["learned"] = {"value": value, "ms_per_step": ms / args.steps, "rel_tol": tau,
+                              "final_rel_residual_median": float(np.median(rel_l)),
+                              "iterations_mean": float(np.mean(used_l)),
+                              "reached_tol_fraction": float(np.mean(np.array(rel_l) <= tau * 1.0001))}
 
     # ---- end to end through the public API with host buffers: per step the
     # frame's writeParams from host memory, one substep, and the positions
@@ -269,8 +332,10 @@ def run_xpbi(args, rank: int, world: int):
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": args.workload, "particles_per_gpu": n_total, "scenes": len(scenes),
-                      "solver": "plain", "iterations": [s["iterations"] for s in scenes][:4],
+                      "solver": args.solver, "preroll_substeps": args.preroll,
+                      "iterations": [s["iterations"] for s in scenes][:4],
                       "l2": "inputs larger than L2 (state ~1.3 GB per 4M particles)"},
+           "solvers": solvers,
            "roofline": roofline, "clocks": clk, "gpu_launches": launches * args.steps,
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}}
     if rank == 0 and not args.no_cpu_baseline:
@@ -294,8 +359,16 @@ def main():
     ap.add_argument("--cpu-scale", type=float, default=0.25)
     ap.add_argument("--profile-substeps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--solver", default=None, choices=["learned", "plain"],
+                    help="learned warm start at the plain solve's residual (default for the dam-breach mix)")
+    ap.add_argument("--preroll", type=int, default=None, help="untimed plain substeps before warm-up")
+    ap.add_argument("--residual-substeps", type=int, default=4)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.solver is None:
+        args.solver = "learned" if args.workload in ("dam_mix4", "dam_breach") else "plain"
+    if args.preroll is None:
+        args.preroll = 100 if args.solver == "learned" else 0
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
     if args.impl == "reference":

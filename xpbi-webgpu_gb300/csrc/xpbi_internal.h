@@ -11,7 +11,7 @@ constexpr uint32_t kKindSnow = 5u;
 constexpr uint32_t kKindWater = 6u;
 
 constexpr uint32_t kNbrCap = 64u;      // neighbour-list capacity per particle
-constexpr int kResidChunks = 16;       // per-scene partial sums of the residual
+constexpr int kResidChunks = 64;       // per-scene partial sums of the residual
 constexpr int kMaxResid = 129;         // residual slots per scene (iterations + 1)
 constexpr int kFeat = 16;              // network features per particle
 
