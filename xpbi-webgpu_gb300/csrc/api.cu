@@ -401,7 +401,7 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
     R.mark(st, "features");
   }
   if (sch.mode == 1) {
-    mlp_forward(b.feat, b.N, b.netBlob, b.netOut, nullptr, s->netErr, st);
+    mlp_forward(b.feat, b.N, b.netBlob, b.netOut, nullptr, s->netErr, st, true);
     R.mark(st, "network");
     launch_warm_from_net(b, st);
     R.mark(st, "warmstart");

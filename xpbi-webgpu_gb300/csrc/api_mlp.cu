@@ -15,7 +15,7 @@ int mlp_param_count();
 size_t mlp_blob_bytes();
 void mlp_pack(const float* dParams, void* dBlob, cudaStream_t st);
 cudaError_t mlp_forward(const float* dX, uint32_t rows, const void* dBlob, float* dY, float* dZ, int* dErr,
-                        cudaStream_t st);
+                        cudaStream_t st, bool skipZero);
 cudaError_t mlp_grad(const float* dX, const float* dT, uint32_t rows, const void* dBlob, float* dY, float* dZ,
                      float* dPartial, float* dSq, float* dGrad, float* dLoss, int* dErr, cudaStream_t st);
 void mlp_adam(float* dW, const float* dG, float* dM, float* dV, float lr, int step, cudaStream_t st);
@@ -75,7 +75,7 @@ int xpbi_mlp_forward(const float* X, uint32_t rows, const float* params, float* 
   MLP_CK(cudaMemcpy(dP, params, sizeof(float) * P, cudaMemcpyHostToDevice));
   MLP_CK(cudaMemset(dE, 0, sizeof(int)));
   mlp_pack(dP, dB, 0);
-  MLP_CK(mlp_forward(dX, rows, dB, dY, nullptr, dE, 0));
+  MLP_CK(mlp_forward(dX, rows, dB, dY, nullptr, dE, 0, false));
   MLP_CK(cudaDeviceSynchronize());
   int rc = deviceErr(dE);
   if (rc) return rc;

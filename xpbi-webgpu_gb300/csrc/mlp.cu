@@ -56,9 +56,11 @@ constexpr uint32_t sW3 = sW2 + kHid * kHid * 2;
 constexpr uint32_t sF32 = sW3 + kHid * kHid * 2;
 constexpr uint32_t kFwdSmem = sF32 + (4 * kHid + 4) * 4;
 
-__device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
+// SiLU z * sigmoid(z) with the MUFU exponential and reciprocal (a few ulp)
+__device__ __forceinline__ float sigm(float z) { return __fdividef(1.f, 1.f + __expf(-z)); }
+__device__ __forceinline__ float silu(float z) { return z * sigm(z); }
 __device__ __forceinline__ float dsilu(float z) {
-  const float s = 1.f / (1.f + __expf(-z));
+  const float s = sigm(z);
   return s * (1.f + z * (1.f - s));
 }
 
@@ -93,7 +95,8 @@ struct FwdOut {
 
 // Forward over `rows` feature rows X[rows][16] (f32).
 __global__ void __launch_bounds__(kRows) k_mlp_fwd(const float* __restrict__ X, uint32_t rows,
-                                                   const uint8_t* __restrict__ blob, FwdOut out, int* err) {
+                                                   const uint8_t* __restrict__ blob, FwdOut out, int* err,
+                                                   int skipZero) {
   extern __shared__ __align__(1024) uint8_t sm[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tbase;
@@ -124,6 +127,7 @@ __global__ void __launch_bounds__(kRows) k_mlp_fwd(const float* __restrict__ X, 
   for (uint32_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     const uint32_t row = tile * kRows + tid;
     // ---- layer 1 input: features as bf16, K = 16
+    bool active = false;
     {
       float x[kIn];
       if (row < rows) {
@@ -138,6 +142,8 @@ __global__ void __launch_bounds__(kRows) k_mlp_fwd(const float* __restrict__ X, 
         for (int q = 0; q < kIn; ++q) x[q] = 0.f;
       }
 #pragma unroll
+      for (int q = 0; q < kIn; ++q) active |= x[q] != 0.f;
+#pragma unroll
       for (int c = 0; c < kIn / 8; ++c) {
         __align__(16) __nv_bfloat16 h[8];
 #pragma unroll
@@ -145,11 +151,17 @@ __global__ void __launch_bounds__(kRows) k_mlp_fwd(const float* __restrict__ X, 
         *reinterpret_cast<uint4*>(sm + sA + tc::coreOffset(tid, 8 * c, kIn)) = *reinterpret_cast<uint4*>(h);
       }
     }
-    float h3[kHid];
+    // the solver's tiles of water particles (all-zero feature rows) need no
+    // prediction: their output is defined as 0
+    if (skipZero && !__syncthreads_or(active)) {
+      if (row < rows) out.y[row] = 0.f;
+      continue;
+    }
+    float y = F[4 * kHid];
     for (int layer = 0; layer < 3 && ok; ++layer) {
       tc::fenceProxyAsync();
       tc::fenceBeforeSync();
-      __syncthreads();
+      __syncthreads();  // A written by every thread; every warp done with the accumulator
       if (tid == 0) {
         tc::fenceAfterSync();
         const uint32_t K = layer == 0 ? kIn : kHid;
@@ -166,40 +178,37 @@ __global__ void __launch_bounds__(kRows) k_mlp_fwd(const float* __restrict__ X, 
       }
       phase ^= 1u;
       tc::fenceAfterSync();
-      // epilogue: this thread's row, 64 columns
-      float z[kHid];
-#pragma unroll
-      for (int c = 0; c < kHid / 16; ++c) tc::ld16(tRow + 16 * c, z + 16 * c);
+      // epilogue, 16 columns of this thread's row at a time; the MMA that read
+      // A has completed, so the next layer's A row is written in place
       const float* bias = F + layer * kHid;
-#pragma unroll
-      for (int j = 0; j < kHid; ++j) z[j] += bias[j];
-      if (out.z != nullptr && row < rows) {
-        float4* zr = reinterpret_cast<float4*>(out.z + ((size_t)layer * rows + row) * kHid);
-#pragma unroll
-        for (int q = 0; q < kHid / 4; ++q) zr[q] = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
-      }
-      tc::fenceBeforeSync();
-      __syncthreads();  // every warp has read the accumulator; A may be overwritten
-      if (layer < 2) {
-#pragma unroll
-        for (int c = 0; c < kHid / 8; ++c) {
-          __align__(16) __nv_bfloat16 h[8];
-#pragma unroll
-          for (int e = 0; e < 8; ++e) h[e] = __float2bfloat16_rn(silu(z[8 * c + e]));
-          *reinterpret_cast<uint4*>(sm + sA + tc::coreOffset(tid, 8 * c, kHid)) = *reinterpret_cast<uint4*>(h);
-        }
-      } else {
-#pragma unroll
-        for (int j = 0; j < kHid; ++j) h3[j] = silu(z[j]);
-      }
-    }
-    if (ok && row < rows) {
       const float* w4 = F + 3 * kHid;
-      float y = F[4 * kHid];
+#pragma unroll 1
+      for (int c = 0; c < kHid / 16; ++c) {
+        float z[16];
+        tc::ld16(tRow + 16 * c, z);
 #pragma unroll
-      for (int j = 0; j < kHid; ++j) y += h3[j] * w4[j];
-      out.y[row] = y;
+        for (int j = 0; j < 16; ++j) z[j] += bias[16 * c + j];
+        if (out.z != nullptr && row < rows) {
+          float4* zr = reinterpret_cast<float4*>(out.z + ((size_t)layer * rows + row) * kHid + 16 * c);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) zr[q] = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+        }
+        if (layer < 2) {
+#pragma unroll
+          for (int h8 = 0; h8 < 2; ++h8) {
+            __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) h[e] = __float2bfloat16_rn(silu(z[8 * h8 + e]));
+            *reinterpret_cast<uint4*>(sm + sA + tc::coreOffset(tid, 16 * c + 8 * h8, kHid)) =
+                *reinterpret_cast<uint4*>(h);
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) y += silu(z[j]) * w4[16 * c + j];
+        }
+      }
     }
+    if (ok && row < rows) out.y[row] = y;
   }
   tc::fenceBeforeSync();
   __syncthreads();
@@ -408,7 +417,7 @@ void mlp_pack(const float* dParams, void* dBlob, cudaStream_t st) {
 }
 
 cudaError_t mlp_forward(const float* dX, uint32_t rows, const void* dBlob, float* dY, float* dZ, int* dErr,
-                        cudaStream_t st) {
+                        cudaStream_t st, bool skipZero) {
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_mlp_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kFwdSmem);
@@ -417,8 +426,10 @@ cudaError_t mlp_forward(const float* dX, uint32_t rows, const void* dBlob, float
   }
   if (rows == 0) return cudaSuccess;
   const uint32_t ntiles = (rows + kRows - 1) / kRows;
-  const uint32_t grid = ntiles < 152u * 4u ? ntiles : 152u * 4u;
-  k_mlp_fwd<<<grid, kRows, kFwdSmem, st>>>(dX, rows, static_cast<const uint8_t*>(dBlob), FwdOut{dY, dZ}, dErr);
+  // 48 registers and 37 KB of shared memory: six CTAs per SM (384 TMEM columns)
+  const uint32_t grid = ntiles < 152u * 6u ? ntiles : 152u * 6u;
+  k_mlp_fwd<<<grid, kRows, kFwdSmem, st>>>(dX, rows, static_cast<const uint8_t*>(dBlob), FwdOut{dY, dZ}, dErr,
+                                           skipZero ? 1 : 0);
   return cudaGetLastError();
 }
 

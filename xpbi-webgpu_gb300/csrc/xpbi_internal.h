@@ -146,8 +146,9 @@ void launch_keep_lambda(const Bufs& b, cudaStream_t st);
 // ---- network (mlp.cu) ----
 size_t mlp_blob_bytes();
 void mlp_pack(const float* dParams, void* dBlob, cudaStream_t st);
+// skipZero: tiles whose 128 feature rows are all zero output 0 without running the network
 cudaError_t mlp_forward(const float* dX, uint32_t rows, const void* dBlob, float* dY, float* dZ, int* dErr,
-                        cudaStream_t st);
+                        cudaStream_t st, bool skipZero = false);
 void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, cudaStream_t st);
 void launch_pbfA(const Bufs& b, int k, const float4* velIn, cudaStream_t st);
 void launch_pbfB(const Bufs& b, int k, const float4* velIn, float4* velOut, cudaStream_t st);
