@@ -230,6 +230,37 @@ int xpbi_mlp_grad(const float* X, const float* T, uint32_t rows, const float* pa
 int xpbi_mlp_train(const float* X, const float* T, uint32_t rows, float* params, int32_t steps, uint32_t batch,
                    float lr, float* loss_history);
 
+/* ---- cell sort without allocation (no counterpart in the reference) ----
+ * For callers that own every byte of device memory and cannot let a library
+ * allocate: engines and plugins that hand out buffers from their own fixed
+ * pool, and code that records work into a CUDA graph, where a cudaMalloc
+ * would break the recording. It runs the substep's first stage alone (cell
+ * key, histogram, scan, bucket fill, deterministic ranks: the same results
+ * as xpbi_encode_substep's sort) on the caller's device buffers, with all
+ * scratch in one fixed array inside this library (about 10 MB per device,
+ * held until the process exits). Nothing is allocated.
+ *   pos4        device, n float4 (x, y, z, any w), 16-byte aligned
+ *   origin, cell_size, dims   host; the grid of xpbi_read_uniforms words
+ *               0..6 (cell = clamp(floor((p - origin) / cell_size), 0, dim-1))
+ *   cell_start  device, out, dims[0]*dims[1]*dims[2] + 1 words, 16-byte
+ *               aligned: start of each cell's run; the last word is n
+ *   sorted_idx  device, out, n words: particle indices in cell order, within
+ *               a cell by descending index
+ *   cuda_stream the stream to enqueue on (NULL: the legacy default stream)
+ * Limits: 1 <= n <= XPBI_NOALLOC_MAX_PARTICLES and at most
+ * XPBI_NOALLOC_MAX_CELLS cells; larger inputs return XPBI_ERR_INVALID.
+ * The first call on a device (with that device current) looks up the
+ * scratch array's address; make it before any stream capture. Each call
+ * clears the parts of the scratch that must start at zero (cell counters,
+ * scan descriptors) itself. Calls share the one array per device: two calls
+ * whose work can overlap on the GPU (other streams, other host threads)
+ * race and corrupt each other's results, so serialise them. Returns after
+ * enqueueing; synchronise the stream before reading the outputs. */
+#define XPBI_NOALLOC_MAX_PARTICLES 262144u
+#define XPBI_NOALLOC_MAX_CELLS 1048576u
+int xpbi_sort_cells_noalloc(const float* pos4, uint32_t n, const float origin[3], float cell_size,
+                            const int32_t dims[3], uint32_t* cell_start, uint32_t* sorted_idx, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -284,4 +284,11 @@ void launch_reorder(const Bufs& b, bool keepLam, cudaStream_t st) {
   k_reorder<<<grid(b.N, kThreads), kThreads, 0, st>>>(b, keepLam ? 1 : 0);
 }
 
+// The crowded-bucket sort alone, with caller-provided scratch of at least
+// 2N words; buckets above the returned member count are left sorted.
+uint32_t launch_bigcells(const Bufs& b, uint32_t* scratch, cudaStream_t st) {
+  k_bigcells<<<kBigGrid, kBigThreads, kSmemSortCap * sizeof(uint32_t), st>>>(b, scratch);
+  return kBigCell;
+}
+
 }  // namespace xpbi
