@@ -196,18 +196,22 @@ def timed_steps(sim, has_water, steps, stream, dist):
 
 
 def residual_stats(sim, has_water, n_scenes, substeps):
-    """Final residual relative to the plain start, and iterations applied,
-    over `substeps` tracked substeps of every scene."""
-    rel, used = [], []
+    """Final constraint and contact residuals relative to their starting
+    values, and iterations applied, over `substeps` tracked substeps of every
+    scene."""
+    rel, relc, used = [], [], []
     for _ in range(substeps):
         sim.step(1, -1, has_water)
         for k in range(n_scenes):
             r, u = sim.read_residuals(k)
+            c = sim.read_contact_residuals(k)
+            K = sim.scenes[k]["iterations"]
             if r[0] > 0:
-                fin = r[1 + sim.scenes[k]["iterations"]]
-                rel.append(float(fin / r[0]))
+                rel.append(float(r[1 + K] / r[0]))
+            if c[0] > 0:
+                relc.append(float(c[1 + K] / c[0]))
             used.append(u)
-    return rel, used
+    return rel, relc, used
 
 
 def run_xpbi(args, rank: int, world: int):
@@ -238,17 +242,19 @@ def run_xpbi(args, rank: int, world: int):
                          "iterations": [s["iterations"] for s in scenes][:4]}}
     ms, value = ms_plain, value_plain
     if learned:
-        # equal residual: the plain solve's own final residual, relative to
-        # its starting residual, median over tracked substeps and scenes
+        # equal residual: the plain solve's own final constraint and contact
+        # residuals, relative to their starting values, median over tracked
+        # substeps and scenes; the learned solve stops once both are reached
         sim.set_solver(0, 0.0, True, True)
-        rel, _ = residual_stats(sim, has_water, len(scenes), args.residual_substeps)
+        rel, relc, _ = residual_stats(sim, has_water, len(scenes), args.residual_substeps)
         tau = float(np.median(rel))
+        tau_c = float(np.median(relc)) if relc else 1.0
         sim.close()
         tw = importlib.import_module("xpbi-webgpu_gb300.train_warm")
         net = tw.load_weights()
         sim, has_water = make_sim(xp, scenes, stream, args.preroll)
         sim.set_network(net)
-        sim.set_solver(1, tau, False, False)
+        sim.set_solver(1, tau, False, False, contact_rel_tol=tau_c)
         sim.step(args.warmup, -1, has_water)
         sim.synchronize()
         clocks = Clocks(local)
@@ -257,28 +263,17 @@ def run_xpbi(args, rank: int, world: int):
         clk = clocks.stop()
         value = n_total * world * args.steps / (ms / 1e3)
         launches = sim.launches_per_substep(-1, has_water)
-        sim.set_solver(1, tau, True, False)
-        rel_l, used_l = residual_stats(sim, has_water, len(scenes), args.residual_substeps)
-        sim.set_solver(1, tau, False, False)
+        sim.set_solver(1, tau, True, False, contact_rel_tol=tau_c)
+        rel_l, relc_l, used_l = residual_stats(sim, has_water, len(scenes), args.residual_substeps)
+        sim.set_solver(1, tau, False, False, contact_rel_tol=tau_c)
         solvers["plain"]["final_rel_residual_median"] = tau
+        solvers["plain"]["final_rel_contact_residual_median"] = tau_c
         solvers["learned"] = {"value": value, "ms_per_step": ms / args.steps, "rel_tol": tau,
+                              "contact_rel_tol": tau_c,
                               "final_rel_residual_median": float(np.median(rel_l)),
+                              "final_rel_contact_residual_median": float(np.median(relc_l)) if relc_l else None,
                               "iterations_mean": float(np.mean(used_l)),
                               "reached_tol_fraction": float(np.mean(np.array(rel_l) <= tau * 1.0001))}
-        # second protocol: a tolerance above the iteration's residual floor,
-        # both solves stopping early at it
-        loose = args.loose_tol
-        for name, mode in (("plain_at_loose_tol", 0), ("learned_at_loose_tol", 1)):
-            sim.set_solver(mode, loose, False, False)
-            sim.step(2, -1, has_water)
-            sim.synchronize()
-            ms_l = timed_steps(sim, has_water, args.steps, stream, dist)
-            sim.set_solver(mode, loose, True, False)
-            rel_x, used_x = residual_stats(sim, has_water, len(scenes), args.residual_substeps)
-            solvers[name] = {"value": n_total * world * args.steps / (ms_l / 1e3), "rel_tol": loose,
-                             "ms_per_step": ms_l / args.steps, "iterations_mean": float(np.mean(used_x)),
-                             "final_rel_residual_median": float(np.median(rel_x))}
-        sim.set_solver(1, tau, False, False)
 
     # ---- end to end through the public API with host buffers: per step the
     # frame's writeParams from host memory, one substep, and the positions
@@ -377,8 +372,6 @@ def main():
                     help="learned warm start at the plain solve's residual (default for the dam-breach mix)")
     ap.add_argument("--preroll", type=int, default=None, help="untimed plain substeps before warm-up")
     ap.add_argument("--residual-substeps", type=int, default=4)
-    ap.add_argument("--loose-tol", type=float, default=1e-2,
-                    help="tolerance of the second protocol (above the residual floor)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.solver is None:

@@ -186,18 +186,27 @@ int xpbi_launches_per_substep(xpbi_sim* sim, int32_t iterations, int32_t has_wat
 
 /* ---- solver modes (no counterpart in the reference) ----
  * mode 0: the reference solve (every XPBI iteration starts from lambda = 0).
- * mode 1: iteration 0 starts from the warm-start network's multiplier.
+ * mode 1: iteration 0 starts from the particle's previous-substep multiplier
+ *   plus the increment the warm-start network predicts.
  * mode 2: iteration 0 starts from the particle's previous-substep multiplier.
  * rel_tol > 0: a scene stops iterating (its remaining passes skip) once its
- *   constraint residual |C + alpha_tilde lambda| falls to rel_tol times
- *   |C| at the predicted velocities; <= 0 keeps the fixed iteration count.
+ *   constraint residual |C + alpha_tilde lambda + gamma dt dC/dt| (0 for an
+ *   inactive constraint, C = 0) falls to rel_tol times its value at
+ *   lambda = 0 and its contact residual (the contact correction solveB would
+ *   apply) to contact_rel_tol times its value entering iteration 0
+ *   (contact_rel_tol < 0: rel_tol); rel_tol <= 0 keeps the fixed iteration
+ *   count. With a warm start the earliest stop is after
+ *   iteration 0. Scheduled PBF passes run whether or not the scene stopped.
  * track_residual: record the residual norm of every iteration and of the
  *   final state (xpbi_read_residuals).
  * log_features: compute the network features every substep
  *   (xpbi_read_training). */
-int xpbi_set_solver(xpbi_sim* sim, int32_t mode, float rel_tol, int32_t track_residual, int32_t log_features);
+int xpbi_set_solver(xpbi_sim* sim, int32_t mode, float rel_tol, float contact_rel_tol, int32_t track_residual,
+                    int32_t log_features);
 
-/* Load the warm-start network's 9473 parameters (layout of xpbi_mlp_*). */
+/* Load the warm-start network's 9473 parameters (layout of xpbi_mlp_*).
+ * Its output is alpha_tilde times the multiplier increment over the previous
+ * substep's final multiplier. */
 int xpbi_set_network(xpbi_sim* sim, const float* params, uint32_t count);
 
 /* Residual norms of the last substep of one scene: norms[0] = |C(v_pred)|,
@@ -206,9 +215,15 @@ int xpbi_set_network(xpbi_sim* sim, const float* params, uint32_t count);
  * *iterations_run = iterations whose update was applied. */
 int xpbi_read_residuals(xpbi_sim* sim, uint32_t scene, double* norms, int32_t cap, int32_t* iterations_run);
 
+/* Contact residual norms of the last substep of one scene, in the slots of
+ * xpbi_read_residuals: the norm of the contact position correction solveB
+ * would apply at each iteration's velocities (norms[0] = iteration 0's). */
+int xpbi_read_contact_residuals(xpbi_sim* sim, uint32_t scene, double* norms, int32_t cap);
+
 /* Training rows of the last substep of one scene (cell-sorted order):
- * features16 [n][16] (zeros for water), target [n] = alpha_tilde * final
- * lambda, *alpha_tilde (may be NULL). Needs log_features or mode 1. */
+ * features16 [n][16] (zeros for water; feature 4 is alpha_tilde times the
+ * previous substep's multiplier), target [n] = alpha_tilde * final lambda,
+ * *alpha_tilde (may be NULL). Needs log_features or mode 1. */
 int xpbi_read_training(xpbi_sim* sim, uint32_t scene, float* features16, float* target, float* alpha_tilde);
 
 /* ---- warm-start network (no counterpart in the reference) ----

@@ -35,7 +35,8 @@ def _curves(xp, sc, st, mode, net=None, substeps=3, tol=0.0):
         for _ in range(substeps):
             sim.encode_substep(it, sc["hasWater"])
             r, used = sim.read_residuals()
-            out.append((r[: it + 2] / r[0], used))
+            c = sim.read_contact_residuals()
+            out.append((r[: it + 2] / r[0], used, c[: it + 2] / c[0] if c[0] > 0 else np.zeros(it + 2)))
         state = sim.read_state()
     return out, state
 
@@ -53,11 +54,12 @@ def test_tracking_does_not_change_the_solve(xp, built_lib):
         assert np.array_equal(res[0][k], res[1][k]), k
 
 
-def test_zero_network_is_the_plain_solve(xp, built_lib):
+def test_zero_network_is_the_previous_multiplier_start(xp, built_lib):
+    """The network predicts an increment over the previous multiplier."""
     sc = xp.scenes.dam_breach()
     zero = np.zeros(9473, np.float32)
     res = []
-    for mode in (0, 1):
+    for mode in (2, 1):
         with xp.Simulation(sc) as sim:
             sim.write_params(xp.params_for(sc))
             sim.set_network(zero)
@@ -72,7 +74,7 @@ def test_plain_residual_history(xp, built_lib):
     sc = xp.scenes.config_sand_column()
     st = _rollout(xp, sc, 300)
     (curves, _), = [_curves(xp, sc, st, 0, substeps=1)]
-    r, used = curves[-1]
+    r, used, _ = curves[-1]
     assert used == sc["iterations"]
     assert r[0] == 1.0 and r[1] == pytest.approx(1.0, rel=1e-6)  # iteration 0 enters at lambda = 0
     assert r[-1] < 0.05 * r[1]  # ten damped Jacobi iterations remove >95% of it
@@ -82,21 +84,24 @@ def test_early_stop_skips_remaining_iterations(xp, built_lib):
     sc = xp.scenes.config_sand_column()
     st = _rollout(xp, sc, 300)
     curves, _ = _curves(xp, sc, st, 0, substeps=2, tol=0.2)
-    for r, used in curves:
+    for r, used, c in curves:
         assert 0 < used < sc["iterations"]
-        assert r[1 + used] <= 0.2 * 1.0001  # the residual that triggered the stop
+        # the residuals that triggered the stop: constraint and contact
+        assert r[1 + used] <= 0.2 * 1.0001 and c[1 + used] <= 0.2 * 1.0001
+        assert r[used] > 0.2 or c[used] > 0.2  # and not one iteration earlier
         assert np.isnan(r[2 + used:-1]).all()
 
 
 def test_network_warm_start_gains(xp, tw):
     """Held-out dam breach (a seed the training scenes never use), 150
     substeps in. What the trained network gains over the method without it:
-    its multiplier starts the solve several times closer to convergence than
-    the plain zero start and than the previous substep's multiplier, and the
-    early iterations stay ahead of the plain solve. What it does not gain
-    here: the damped Jacobi iteration ends on a residual floor set by the
-    contact and PBF corrections, which the warm-started solve reaches about
-    as late as the plain one (printed, not asserted)."""
+    its multiplier starts the solve many times closer to convergence than the
+    plain zero start and clearly closer than the previous substep's
+    multiplier alone, and the early iterations stay ahead of the plain solve.
+    What it does not gain: the contact correction that runs inside the same
+    iterations converges at the same rate from any multiplier start, so the
+    contact residual curves coincide and set the iterations an equal-residual
+    stop needs (printed, not asserted)."""
     net = tw.load_weights()
     sc = xp.scenes.config_dam_breach(seed=0, scale=0.1)
     st = _rollout(xp, sc, 150)
@@ -104,10 +109,11 @@ def test_network_warm_start_gains(xp, tw):
     prev, _ = _curves(xp, sc, st, 2)
     learned, _ = _curves(xp, sc, st, 1, net)
     it = sc["iterations"]
-    for (rp, _), (rv, _), (rl, _) in zip(plain, prev, learned):
-        assert rl[1] < 0.5 * rv[1] < 0.5 * rp[1]   # starting residual
+    for (rp, _, cp), (rv, _, _), (rl, _, cl) in zip(plain, prev, learned):
+        assert rl[1] < 0.6 * rv[1] and rv[1] < 0.5 * rp[1]  # starting residual
         assert (rl[1:5] < rp[1:5]).all()              # ahead in the first iterations
-        assert rl[-1] < 3.0 * rp[-1]                  # no worse floor than 3x plain's
+        assert rl[-1] < 3.0 * rp[-1]                  # final residual no worse than 3x plain's
+        print("contact residual after the budget: plain", float(cp[-1]), "network", float(cl[-1]))
         target = rp[-1] * 1.05                        # plain's final residual
         k_plain = int(np.argmax(rp[1:it + 1] <= target)) if (rp[1:it + 1] <= target).any() else it
         k_net = int(np.argmax(rl[1:it + 1] <= target)) if (rl[1:it + 1] <= target).any() else it

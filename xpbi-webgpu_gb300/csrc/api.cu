@@ -274,6 +274,7 @@ struct xpbi_sim {
   // solver mode: 0 plain (reference), 1 network warm start, 2 previous-multiplier warm start
   int mode = 0;
   float residTol = 0.f;     // early stop tolerance relative to |C(v_pred)|; <= 0 off
+  float residTolC = 0.f;    // the contact residual's tolerance
   bool track = false;       // residual history per iteration
   bool features = false;    // compute network features every substep (training logs)
   bool netLoaded = false;
@@ -317,6 +318,7 @@ int upload(xpbi_sim* s) {
   for (uint32_t i = 0; i < S; ++i) {
     buildSceneDev(s->sc[i], i, s->sdev[i], &s->mdev[(size_t)i * kMaxMats]);
     s->sdev[i].residTol = s->residTol;
+    s->sdev[i].residTolC = s->residTolC;
     for (uint32_t m = 0; m < s->sc[i].nMats; ++m)
       packMaterial(s->sc[i].mats[m], s->sc[i].V0, &s->matWordsHost[((size_t)i * kMaxMats + m) * XPBI_MATERIAL_WORDS]);
   }
@@ -419,7 +421,7 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
     launch_solveA(b, k, b.velS[in], aflags, st);
     R.mark(st, "solveA");
     if (sch.reduce) {
-      launch_resid_reduce(b, k, st);
+      launch_resid_reduce(b, k, (aflags & kWarm) != 0, st);
       R.mark(st, "residual");
     }
     launch_solveB(b, k, b.velS[in], b.velS[in ^ 1], sch.pbf[k] != 0, st);
@@ -436,7 +438,7 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
   if (sch.track) {  // residual of the state the iterations leave behind
     launch_solveA(b, sch.K, b.velS[in], kTrackResid | kMeasureOnly, st);
     R.mark(st, "solveA(measure)");
-    launch_resid_reduce(b, -1, st);
+    launch_resid_reduce(b, -1, false, st);
     R.mark(st, "residual");
   }
   launch_xsph(b, b.velS[in], b.velS[in ^ 1], st);
@@ -545,9 +547,12 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   A(b.netOut, n);
   A(b.rr, n);
   A(b.c0sq, n);
-  A(b.residPart, (size_t)nScenes * kResidChunks * 2);
+  A(b.rc, n);
+  A(b.residPart, (size_t)nScenes * kResidChunks * 3);
   A(b.resid, (size_t)nScenes * kMaxResid);
+  A(b.residC, (size_t)nScenes * kMaxResid);
   A(b.c0, nScenes);
+  A(b.cc0, nScenes);
   A(b.done, nScenes);
   A(b.itersUsed, nScenes);
   {
@@ -597,6 +602,8 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
             cudaMemset(b.done, 0, sizeof(int) * nScenes) == cudaSuccess &&
             cudaMemset(b.itersUsed, 0, sizeof(int) * nScenes) == cudaSuccess &&
             cudaMemset(b.resid, 0, sizeof(double) * nScenes * kMaxResid) == cudaSuccess &&
+            cudaMemset(b.residC, 0, sizeof(double) * nScenes * kMaxResid) == cudaSuccess &&
+            cudaMemset(b.cc0, 0, sizeof(double) * nScenes) == cudaSuccess &&
             cudaMemset(s->netErr, 0, sizeof(int)) == cudaSuccess &&
             cudaMemset(b.cellStart, 0, 4 * ((size_t)b.C + 4)) == cudaSuccess;
   if (!ok) return bail(fail(XPBI_ERR_CUDA, "initial upload failed"));
@@ -968,13 +975,17 @@ int xpbi_device_ptrs(xpbi_sim* sim, void** pos4, void** vel4, void** materials) 
   return XPBI_OK;
 }
 
-int xpbi_set_solver(xpbi_sim* sim, int32_t mode, float rel_tol, int32_t track_residual, int32_t log_features) {
+int xpbi_set_solver(xpbi_sim* sim, int32_t mode, float rel_tol, float contact_rel_tol, int32_t track_residual,
+                    int32_t log_features) {
   XPBI_TRY(checkSim(sim));
   if (mode < 0 || mode > 2) return fail(XPBI_ERR_INVALID, "solver mode must be 0, 1 or 2");
   if (mode == 1 && !sim->netLoaded) return fail(XPBI_ERR_INVALID, "network warm start needs xpbi_set_network first");
   if (!(rel_tol <= 1.f) || !std::isfinite(rel_tol)) return fail(XPBI_ERR_INVALID, "rel_tol must be <= 1");
+  if (!(contact_rel_tol <= 1.f) || !std::isfinite(contact_rel_tol))
+    return fail(XPBI_ERR_INVALID, "contact_rel_tol must be <= 1");
   sim->mode = mode;
   sim->residTol = rel_tol;
+  sim->residTolC = contact_rel_tol < 0.f ? rel_tol : contact_rel_tol;
   sim->track = track_residual != 0;
   sim->features = log_features != 0;
   sim->dirty = true;
@@ -1007,6 +1018,29 @@ int xpbi_read_residuals(xpbi_sim* sim, uint32_t scene, double* norms, int32_t ca
   if (iterations_run) *iterations_run = used;
   if (norms && cap > 0) {
     // [ |C(v_pred)|, |r_0| .. |r_{K-1}|, |r| after the last applied iteration ]
+    std::vector<double> out;
+    out.push_back(std::sqrt(c0));
+    for (int k = 0; k < K && k < kMaxResid - 1; ++k) out.push_back(k < used + 1 ? std::sqrt(r[k]) : NAN);
+    out.push_back(std::sqrt(r[kMaxResid - 1]));
+    for (int q = 0; q < cap && q < (int)out.size(); ++q) norms[q] = out[q];
+  }
+  return XPBI_OK;
+}
+
+int xpbi_read_contact_residuals(xpbi_sim* sim, uint32_t scene, double* norms, int32_t cap) {
+  XPBI_TRY(checkSim(sim));
+  if (scene >= sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
+  XPBI_TRY(xpbi_synchronize(sim));
+  std::vector<double> r(kMaxResid);
+  double c0 = 0;
+  int used = 0;
+  XPBI_CK(cudaMemcpy(r.data(), sim->b.residC + (size_t)scene * kMaxResid, sizeof(double) * kMaxResid,
+                     cudaMemcpyDeviceToHost));
+  XPBI_CK(cudaMemcpy(&c0, sim->b.cc0 + scene, sizeof(double), cudaMemcpyDeviceToHost));
+  XPBI_CK(cudaMemcpy(&used, sim->b.itersUsed + scene, sizeof(int), cudaMemcpyDeviceToHost));
+  const int K = sim->sc[scene].iterations;
+  if (norms && cap > 0) {
+    // same slots as xpbi_read_residuals; slot 0 repeats iteration 0's value
     std::vector<double> out;
     out.push_back(std::sqrt(c0));
     for (int k = 0; k < K && k < kMaxResid - 1; ++k) out.push_back(k < used + 1 ? std::sqrt(r[k]) : NAN);

@@ -250,8 +250,12 @@ struct Constraint {
   V3 sgrad;       // self gradient (per unit multiplier)
   V3 logSigTr;    // log of the trial singular values (clamped like safeSig)
   float nNbr;     // solid neighbours in the sweep
+  float contact2; // |contact correction|^2 solveB would apply at these velocities (kContact only)
 };
 
+// kContact: also form the contact position correction of the same state
+// (the sum solveB applies, simkernels.js:340-356) for the contact residual.
+template <bool kContact = false>
 __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& cx, uint32_t i, float4 pi,
                                                      const float4* __restrict__ velIn, const MatDev& m, float st) {
   const SceneDev& S = *cx.scene;
@@ -262,6 +266,9 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
   M3 G = mzero();
   V3 sv = splat(0.f);
   float q00 = 0.f, q11 = 0.f, q22 = 0.f, q01 = 0.f, q02 = 0.f, q12 = 0.f, cnt = 0.f;
+  V3 corr = splat(0.f);
+  const V3 xci = xi + S.dt * vi;
+  const float massI = cx.mats[matOfW(pi.w)].mass;
   forNbrs(b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
           [&](uint32_t, bool water, const PV& d) {
             if (water) return;
@@ -270,7 +277,16 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
             const V3 dv = (xyz(d.v) - vi) * Vb;
             G = madd(G, M3{{dv * gt.x, dv * gt.y, dv * gt.z}});
             sv = sv + gt * Vb;
-            const float c = Vb * Vb / cx.mats[matOfW(d.p.w)].mass;
+            const float mb = cx.mats[matOfW(d.p.w)].mass;
+            if (kContact) {
+              const V3 dxc = xci - (xyz(d.p) + S.dt * xyz(d.v));
+              const float d2 = dot(dxc, dxc);
+              if (d2 < S.minD * S.minD && d2 > 1e-18f) {
+                const float rinv = rsqrtf(d2);
+                corr = corr + dxc * (rinv * ((S.minD - d2 * rinv) * (mb / (massI + mb))));
+              }
+            }
+            const float c = Vb * Vb / mb;
             const V3 cg = gt * c;
             q00 += cg.x * gt.x;
             q11 += cg.y * gt.y;
@@ -282,6 +298,7 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
           });
   Constraint out;
   out.nNbr = cnt;
+  out.contact2 = dot(corr, corr);
   const M3 Fn = loadM(b.FS, b.N, i);
   const M3 Ftr = mul(madd(mident(), mscale(G, S.dt)), Fn);
   const SVD sd = svd3Fast(Ftr);
@@ -322,8 +339,12 @@ __device__ __forceinline__ bool sceneDone(const Bufs& b, uint32_t i) {
 // flags & kTrackResid: writes r^2 for the residual of the state entering
 //   this iteration, r = C + alphaT lambda + gamma dt cdot (the numerator the
 //   damped update drives to zero; without the damping term the Jacobi fixed
-//   point sits at C + alphaT lambda = -gamma dt cdot, not 0), and at
-//   iteration 0 the residual at lambda = 0 to c0sq.
+//   point sits at C + alphaT lambda = -gamma dt cdot, not 0), 0 for an
+//   inactive constraint (C = 0), and at iteration 0 the residual at
+//   lambda = 0 to c0sq; also |contact correction|^2 of the same state to rc
+//   (the contact constraints the iteration solves beside the multipliers).
+//   The tracked variant is a separate instantiation (kTrack) so the plain
+//   path carries none of it.
 // flags & kWarm (iteration 0): starts from lambda0 = lamWarm instead of 0.
 //   Its impulse has not been applied to the velocities this pass sees, so the
 //   first correction uses the linearised post-impulse residual: applying
@@ -336,12 +357,13 @@ __device__ __forceinline__ bool sceneDone(const Bufs& b, uint32_t i) {
 //   replaced by the plain start lambda0 = 0 (the plain solve stays the
 //   fallback). With lambda0 = 0 both updates are the reference's.
 // flags & kMeasureOnly: residual only (the pass after the last iteration).
+template <bool kTrack>
 __global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4* __restrict__ velIn, int flags) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
-  const bool track = (flags & kTrackResid) != 0;
+  constexpr bool track = kTrack;
   const bool measure = (flags & kMeasureOnly) != 0;
   const bool warm0 = (flags & kWarm) != 0 && k == 0;
   const float4 pi = b.posS[i];
@@ -349,6 +371,7 @@ __global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4
   if (!active || waterW(pi.w)) {  // water: Sp is never read
     if (track) {
       b.rr[i] = 0.f;
+      b.rc[i] = 0.f;
       if (k == 0) b.c0sq[i] = 0.f;
     }
     return;
@@ -356,7 +379,7 @@ __global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4
   const uint32_t mi = matOfW(pi.w);
   const float st = b.stateS[i];
   const MatDev m = hardenedMat(cx.mats[mi], st);
-  const Constraint c = evalConstraint(b, cx, i, pi, velIn, m, st);
+  const Constraint c = evalConstraint<kTrack>(b, cx, i, pi, velIn, m, st);
   const float g = S.kDamp;
   const float stiff = (1.f + g) * c.denom + S.alphaT;  // d(residual) / d(applied multiplier)
   const float r0 = c.C + g * S.dt * c.cdot;            // residual at lambda = 0
@@ -365,8 +388,12 @@ __global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4
   // the quantity the update drives to zero: r = C + alphaT lambda + gamma dt cdot
   const float lamTerm = warm0 ? stiff * lam0 : S.alphaT * lam0;
   if (track) {
-    const float r = r0 + lamTerm;
+    // an inactive constraint (C below 1e-7: the reference skips the particle
+    // and leaves its multiplier alone) has no residual; counting alphaT lambda
+    // there would add a term no iteration can change
+    const float r = c.C == 0.f ? 0.f : r0 + lamTerm;
     b.rr[i] = r * r;
+    b.rc[i] = c.contact2;
     if (k == 0) b.c0sq[i] = r0 * r0;
   }
   if (measure) return;
@@ -423,13 +450,14 @@ __global__ void __launch_bounds__(kThreads) k_features(Bufs b, const float4* __r
   for (int q = 0; q < kFeat / 4; ++q) out[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
 }
 
-// lambda_warm = network output / alphaT (the network predicts alphaT lambda)
+// lambda_warm = previous multiplier + network output / alphaT (the network
+// predicts alphaT times the increment over the previous substep's multiplier)
 __global__ void k_warm_from_net(Bufs b) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
   const float4 pi = b.posS[i];
-  b.lamWarm[i] = waterW(pi.w) ? 0.f : b.netOut[i] / cx.scene->alphaT;
+  b.lamWarm[i] = waterW(pi.w) ? 0.f : b.lamPrev[i] + b.netOut[i] / cx.scene->alphaT;
 }
 
 // warm start from the previous substep's multiplier alone (no network)
@@ -441,56 +469,72 @@ __global__ void k_warm_from_prev(Bufs b) {
 
 // Per-scene residual norms, deterministic: block (c, s) sums chunk c of
 // scene s in a fixed order; k_resid_final adds the chunks in order.
+// Sums: constraint residual^2, (iteration 0) residual^2 at lambda = 0,
+// contact correction^2.
+constexpr int kResidSums = 3;
 __global__ void __launch_bounds__(256) k_resid_partial(Bufs b, int k) {
-  __shared__ double red[2][256];
+  __shared__ double red[kResidSums][256];
   const uint32_t s = blockIdx.y, c = blockIdx.x;
   const SceneDev& S = b.scenes[s];
   const uint32_t n = S.n, base = S.pBase;
   const uint32_t lo = base + (uint32_t)(((uint64_t)n * c) / kResidChunks);
   const uint32_t hi = base + (uint32_t)(((uint64_t)n * (c + 1)) / kResidChunks);
-  double a = 0.0, a0 = 0.0;
+  double a = 0.0, a0 = 0.0, ac = 0.0;
   if (!b.done[s] || k < 0) {
     for (uint32_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
       a += (double)b.rr[p];
+      ac += (double)b.rc[p];
       if (k == 0) a0 += (double)b.c0sq[p];
     }
   }
   red[0][threadIdx.x] = a;
   red[1][threadIdx.x] = a0;
+  red[2][threadIdx.x] = ac;
   __syncthreads();
   for (int w = 128; w > 0; w >>= 1) {
     if ((int)threadIdx.x < w) {
-      red[0][threadIdx.x] += red[0][threadIdx.x + w];
-      red[1][threadIdx.x] += red[1][threadIdx.x + w];
+#pragma unroll
+      for (int q = 0; q < kResidSums; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + w];
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    b.residPart[(s * kResidChunks + c) * 2] = red[0][0];
-    b.residPart[(s * kResidChunks + c) * 2 + 1] = red[1][0];
-  }
+  if (threadIdx.x < kResidSums) b.residPart[(s * kResidChunks + c) * kResidSums + threadIdx.x] = red[threadIdx.x][0];
 }
 
-// k >= 0: iteration k's residual (early stop); k < 0: after the last
-// iteration (slot kMaxResid - 1).
-__global__ void k_resid_final(Bufs b, int k) {
+// k >= 0: iteration k's residuals (early stop); k < 0: after the last
+// iteration (slot kMaxResid - 1). A scene stops once both its constraint
+// residual and its contact residual are within tol of their values entering
+// iteration 0 (an early stop also ends the contact passes, which the
+// constraint residual does not see). With a warm start, iteration 0's
+// constraint residual is the linearised estimate before the warm impulse is
+// applied, so the earliest stop is after iteration 0.
+__global__ void k_resid_final(Bufs b, int k, int warm) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= b.S) return;
   const SceneDev& S = b.scenes[s];
   if (k >= 0 && (b.done[s] || k >= S.iterations)) return;
-  double a = 0.0, a0 = 0.0;
+  double a = 0.0, a0 = 0.0, ac = 0.0;
   for (int c = 0; c < kResidChunks; ++c) {
-    a += b.residPart[(s * kResidChunks + c) * 2];
-    a0 += b.residPart[(s * kResidChunks + c) * 2 + 1];
+    const double* part = b.residPart + (s * kResidChunks + c) * kResidSums;
+    a += part[0];
+    a0 += part[1];
+    ac += part[2];
   }
   if (k < 0) {
     b.resid[(size_t)s * kMaxResid + (kMaxResid - 1)] = a;
+    b.residC[(size_t)s * kMaxResid + (kMaxResid - 1)] = ac;
     return;
   }
-  if (k < kMaxResid - 1) b.resid[(size_t)s * kMaxResid + k] = a;
-  if (k == 0) b.c0[s] = a0;
-  const double tol = (double)S.residTol;
-  if (tol > 0.0 && a <= tol * tol * b.c0[s]) {
+  if (k < kMaxResid - 1) {
+    b.resid[(size_t)s * kMaxResid + k] = a;
+    b.residC[(size_t)s * kMaxResid + k] = ac;
+  }
+  if (k == 0) {
+    b.c0[s] = a0;
+    b.cc0[s] = ac;
+  }
+  const double tol = (double)S.residTol, tolC = (double)S.residTolC;
+  if (tol > 0.0 && a <= tol * tol * b.c0[s] && ac <= tolC * tolC * b.cc0[s] && !(warm && k == 0)) {
     b.done[s] = 1;
     b.itersUsed[s] = k;
   } else {
@@ -824,16 +868,19 @@ inline unsigned grid(uint32_t n) { return (unsigned)((n + kThreads - 1) / kThrea
 
 void launch_computeL(const Bufs& b, cudaStream_t st) { k_computeL<<<grid(b.N), kThreads, 0, st>>>(b); }
 void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, cudaStream_t st) {
-  k_solveA<<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, flags);
+  if (flags & kTrackResid)
+    k_solveA<true><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, flags);
+  else
+    k_solveA<false><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, flags);
 }
 void launch_features(const Bufs& b, const float4* velIn, cudaStream_t st) {
   k_features<<<grid(b.N), kThreads, 0, st>>>(b, velIn);
 }
 void launch_warm_from_net(const Bufs& b, cudaStream_t st) { k_warm_from_net<<<grid(b.N), kThreads, 0, st>>>(b); }
 void launch_warm_from_prev(const Bufs& b, cudaStream_t st) { k_warm_from_prev<<<grid(b.N), kThreads, 0, st>>>(b); }
-void launch_resid_reduce(const Bufs& b, int k, cudaStream_t st) {
+void launch_resid_reduce(const Bufs& b, int k, bool warm, cudaStream_t st) {
   k_resid_partial<<<dim3(kResidChunks, b.S), 256, 0, st>>>(b, k);
-  k_resid_final<<<(b.S + 127) / 128, 128, 0, st>>>(b, k);
+  k_resid_final<<<(b.S + 127) / 128, 128, 0, st>>>(b, k, warm ? 1 : 0);
 }
 void launch_keep_lambda(const Bufs& b, cudaStream_t st) { k_keep_lambda<<<grid(b.N), kThreads, 0, st>>>(b); }
 void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, cudaStream_t st) {

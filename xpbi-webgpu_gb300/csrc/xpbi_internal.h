@@ -64,6 +64,7 @@ struct SceneDev {
   int pbfIterations;        // PBF passes (first k iterations)
   int hasWater;
   float residTol;           // early stop at |r_k| <= residTol |C(v_pred)|; <= 0: never
+  float residTolC;          // ... and |contact_k| <= residTolC |contact_0|
 };
 
 struct MatDev {
@@ -114,9 +115,12 @@ struct Bufs {
   float* netOut;        // [N] network output
   float* rr;            // [N] squared constraint residual of the current iteration
   float* c0sq;          // [N] squared constraint value at the predicted velocities
-  double* residPart;    // [S][kResidChunks] partial sums
+  float* rc;            // [N] squared contact correction of the current iteration
+  double* residPart;    // [S][kResidChunks][3] partial sums
   double* resid;        // [S][kMaxResid] residual norm^2 per iteration (last slot: after the last)
+  double* residC;       // [S][kMaxResid] contact residual norm^2, same slots
   double* c0;           // [S] |C(v_pred)|^2
+  double* cc0;          // [S] contact residual^2 entering iteration 0
   int* done;            // [S] converged: later iterations skip
   int* itersUsed;       // [S] iterations whose update was applied
   void* netBlob;        // packed network weights
@@ -140,7 +144,7 @@ void launch_computeL(const Bufs& b, cudaStream_t st);
 void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, cudaStream_t st);
 void launch_features(const Bufs& b, const float4* velIn, cudaStream_t st);
 void launch_warm_from_net(const Bufs& b, cudaStream_t st);
-void launch_resid_reduce(const Bufs& b, int k, cudaStream_t st);
+void launch_resid_reduce(const Bufs& b, int k, bool warm, cudaStream_t st);
 void launch_keep_lambda(const Bufs& b, cudaStream_t st);
 
 // ---- network (mlp.cu) ----

@@ -241,8 +241,9 @@ class Simulation:
     PLAIN, NETWORK, PREVIOUS = 0, 1, 2
 
     def set_solver(self, mode: int = 0, rel_tol: float = 0.0, track_residual: bool = False,
-                   log_features: bool = False):
-        check(lib().xpbi_set_solver(self._h, mode, rel_tol, 1 if track_residual else 0, 1 if log_features else 0))
+                   log_features: bool = False, contact_rel_tol: float = -1.0):
+        check(lib().xpbi_set_solver(self._h, mode, rel_tol, contact_rel_tol, 1 if track_residual else 0,
+                                    1 if log_features else 0))
 
     def set_network(self, params):
         p = np.ascontiguousarray(params, np.float32)
@@ -259,6 +260,12 @@ class Simulation:
                                         C.byref(used)))
         del it
         return out, used.value
+
+    def read_contact_residuals(self, scene: int = 0):
+        """Contact residual norms in the slots of read_residuals."""
+        out = np.full(256, np.nan)
+        check(lib().xpbi_read_contact_residuals(self._h, scene, out.ctypes.data_as(C.POINTER(C.c_double)), 256))
+        return out
 
     def read_training(self, scene: int = 0):
         n = self.scene_sizes[scene]

@@ -4,13 +4,17 @@ Data: seeded dam-breach scenes (PBF water beside Drucker-Prager sand, the
 benchmark's scene mix) at reduced size with varied sand parameters. Each
 scene runs the plain solve (every iteration from lambda = 0) for a random
 number of substeps, then logs a few substeps: per solid particle the 16
-features at iteration 0 and the target alpha_tilde * lambda after the full
-iteration budget.
+features at iteration 0 and alpha_tilde * lambda after the full iteration
+budget. The network learns the increment of that over the previous
+substep's multiplier (feature 4): the warm start is the previous multiplier
+plus the prediction, so a network that predicts nothing is the
+previous-multiplier start and the BF16 rounding only touches the increment.
 
 Training: Adam with the library's own tensor-core forward / backward
 kernels (xpbi_mlp_train). Inputs and target are standardised for training;
 the affine maps are folded into the first and last layers afterwards, so
-the stored network takes raw features and returns alpha_tilde * lambda.
+the stored network takes raw features and returns alpha_tilde times the
+multiplier increment.
 
     python -m xpbi-webgpu_gb300.train_warm --out weights.bin
 """
@@ -122,6 +126,7 @@ def main():
     ap.add_argument("--out", default=WEIGHTS)
     args = ap.parse_args()
     X, Y = generate(args.scenes, args.scale)
+    Y = Y - X[:, 4]  # increment over the previous substep's multiplier
     print("rows", len(X), "target mean/std", float(Y.mean()), float(Y.std()), flush=True)
     p, hist = fit_network(X, Y, steps=args.steps)
     print("loss (standardised) first / last", float(hist[:20].mean()), float(hist[-20:].mean()), flush=True)
