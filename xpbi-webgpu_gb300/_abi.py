@@ -10,7 +10,8 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libxpbi.so")
+# XPBI_LIB selects another build of the same library (a tuning variant)
+LIB_PATH = os.environ.get("XPBI_LIB") or os.path.join(HERE, "libxpbi.so")
 
 PARAMS_WORDS = 64
 MATERIAL_WORDS = 16

@@ -43,9 +43,15 @@ def _stale(obj: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, ptxas_v: bool = False, force: bool = False) -> str:
-    """Compile every .cu for sm_103a and link libxpbi.so; returns its path."""
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose: bool = False, ptxas_v: bool = False, force: bool = False, out: str | None = None,
+          extra: list[str] | None = None, build_dir: str | None = None) -> str:
+    """Compile every .cu for sm_103a and link libxpbi.so; returns its path.
+
+    out / build_dir / extra (nvcc flags such as -DXPBI_MINB_SOLVEB=8) build
+    a variant of the library elsewhere without touching the default one."""
+    lib = out or LIB
+    bdir = build_dir or BUILD
+    os.makedirs(bdir, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "xpbi.h"))
     exe = nvcc()
@@ -53,10 +59,10 @@ def build(verbose: bool = False, ptxas_v: bool = False, force: bool = False) -> 
     objs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(bdir, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s, *headers, __file__]):
-            cmd = [exe, *_flags(["-Xptxas", "-v"] if ptxas_v else None), "-c", s, "-o", o]
+            cmd = [exe, *_flags((["-Xptxas", "-v"] if ptxas_v else []) + (extra or [])), "-c", s, "-o", o]
             jobs.append(cmd)
 
     def run(cmd: list[str]) -> tuple[list[str], subprocess.CompletedProcess]:
@@ -68,14 +74,14 @@ def build(verbose: bool = False, ptxas_v: bool = False, force: bool = False) -> 
                 sys.stderr.write(r.stdout + r.stderr)
             if r.returncode != 0:
                 raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
-    if jobs or not os.path.exists(LIB) or _stale(LIB, objs):
-        tmp = LIB + ".tmp"
+    if jobs or not os.path.exists(lib) or _stale(lib, objs):
+        tmp = lib + ".tmp"
         cmd = [exe, "-shared", *ARCH, "-o", tmp, *objs]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

@@ -521,7 +521,8 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   A(b.L, 9 * n);
   A(b.lam, n);
   A(b.pbfLam, n);
-  A(b.Sp, 3 * n);
+  A(b.Sp, 4 * n);
+  A(b.SpSelf, n);
   A(b.key, n);
   A(b.tmp, n);
   A(b.sortedIdx, n);

@@ -37,6 +37,38 @@ namespace {
 
 constexpr int kThreads = 128;
 
+// Launch bounds of the stencil kernels: defining XPBI_MINB_<KERNEL> at build
+// time asks the register allocator for that many resident CTAs per SM
+// (trading registers for occupancy); otherwise only the block size is fixed.
+#define XPBI_LB_DEFAULT __launch_bounds__(kThreads)
+#ifdef XPBI_MINB_COMPUTEL
+#define XPBI_LB_COMPUTEL __launch_bounds__(kThreads, XPBI_MINB_COMPUTEL)
+#else
+#define XPBI_LB_COMPUTEL XPBI_LB_DEFAULT
+#endif
+// solveA: 7 CTAs per SM (72 registers, a few spills outside the neighbour
+// loop) measured 15% faster than the allocator's own choice (88 registers,
+// 5 CTAs) on the 4M-particle dam-breach mix; 8 CTAs (64) spills in the loop
+#ifndef XPBI_MINB_SOLVEA
+#define XPBI_MINB_SOLVEA 7
+#endif
+#define XPBI_LB_SOLVEA __launch_bounds__(kThreads, XPBI_MINB_SOLVEA)
+#ifdef XPBI_MINB_SOLVEB
+#define XPBI_LB_SOLVEB __launch_bounds__(kThreads, XPBI_MINB_SOLVEB)
+#else
+#define XPBI_LB_SOLVEB XPBI_LB_DEFAULT
+#endif
+#ifdef XPBI_MINB_PBF
+#define XPBI_LB_PBF __launch_bounds__(kThreads, XPBI_MINB_PBF)
+#else
+#define XPBI_LB_PBF XPBI_LB_DEFAULT
+#endif
+#ifdef XPBI_MINB_UPDATE
+#define XPBI_LB_UPDATE __launch_bounds__(kThreads, XPBI_MINB_UPDATE)
+#else
+#define XPBI_LB_UPDATE XPBI_LB_DEFAULT
+#endif
+
 struct Ctx {
   const SceneDev* __restrict__ scene;
   const MatDev* __restrict__ mats;  // this scene's 8 materials
@@ -97,7 +129,9 @@ __device__ __forceinline__ uint32_t lane4(const uint4& q, uint32_t s) {
   return s == 0u ? q.x : (s == 1u ? q.y : (s == 2u ? q.z : q.w));
 }
 
-template <class Gather, class Body>
+// kRaw: gather() receives the raw entry (index | water bit), e.g. to skip
+// the loads of entries the body ignores.
+template <bool kRaw = false, class Gather, class Body>
 __device__ __forceinline__ void forList(const uint32_t* __restrict__ list, uint32_t cnt, Gather&& gather,
                                         Body&& body) {
   if (cnt == 0) return;
@@ -105,7 +139,7 @@ __device__ __forceinline__ void forList(const uint32_t* __restrict__ list, uint3
   uint4 cur = __ldg(L);
   uint4 nxt = cnt > 4u ? __ldg(L + 1) : cur;
   uint32_t e = cur.x;
-  auto d = gather(e & ~kWaterBit);
+  auto d = gather(kRaw ? e : e & ~kWaterBit);
 #pragma unroll 1
   for (uint32_t k = 1; k < cnt; ++k) {
     const uint32_t sl = k & 3u;
@@ -114,7 +148,7 @@ __device__ __forceinline__ void forList(const uint32_t* __restrict__ list, uint3
       if (k + 4u < cnt) nxt = __ldg(L + (k >> 2) + 1);
     }
     const uint32_t en = lane4(cur, sl);
-    auto dn = gather(en & ~kWaterBit);
+    auto dn = gather(kRaw ? en : en & ~kWaterBit);
     body(e & ~kWaterBit, (e & kWaterBit) != 0u, d);
     e = en;
     d = dn;
@@ -123,9 +157,6 @@ __device__ __forceinline__ void forList(const uint32_t* __restrict__ list, uint3
 }
 
 __device__ __forceinline__ uint32_t* listOf(uint32_t* base, uint32_t i) { return base + (size_t)i * kNbrCap; }
-__device__ __forceinline__ const uint32_t* listOf(const uint32_t* base, uint32_t i) {
-  return base + (size_t)i * kNbrCap;
-}
 
 // In-support neighbours of slot i in stencil order: body(j, jIsWater, data).
 template <class Gather, class Body>
@@ -169,7 +200,7 @@ __device__ __forceinline__ uint32_t recordCandidates(const SceneDev& S, const ui
 // ---------------------------------------------------------------- computeL
 // Bonet-Lok correction with SVD pseudo-inverse (simkernels.js:189-221); its
 // candidate walk records the substep's neighbour list.
-__global__ void __launch_bounds__(kThreads) k_computeL(Bufs b) {
+__global__ void XPBI_LB_COMPUTEL k_computeL(Bufs b) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
@@ -203,10 +234,20 @@ __global__ void __launch_bounds__(kThreads) k_computeL(Bufs b) {
   storeM(b.L, b.N, i, diagMul(s.V, inv, s.U));
 }
 
-__device__ __forceinline__ void storeSp(float4* __restrict__ Sp, uint32_t i, const M3& m, V3 s) {
-  Sp[3 * (size_t)i] = make_float4(m.c[0].x, m.c[0].y, m.c[0].z, s.x);
-  Sp[3 * (size_t)i + 1] = make_float4(m.c[1].x, m.c[1].y, m.c[1].z, s.y);
-  Sp[3 * (size_t)i + 2] = make_float4(m.c[2].x, m.c[2].y, m.c[2].z, s.z);
+// The record solveB gathers from each solid neighbour, in four float4
+// planes (plane f of slot i at Sp[f N + i]) so that one warp-wide gather of
+// a field touches as few cache lines as the neighbour indices allow: dlam
+// G L columns with the position in .w, then the position predicted with the
+// velocities entering this iteration and the mass (the contact pass's
+// inputs). The particle's own dv goes to SpSelf.
+__device__ __forceinline__ void storeSp(const Bufs& b, uint32_t i, const M3& m, V3 self, V3 x, V3 xc, float mass) {
+  float4* __restrict__ R = b.Sp + i;
+  const size_t N = b.N;
+  R[0] = make_float4(m.c[0].x, m.c[0].y, m.c[0].z, x.x);
+  R[N] = make_float4(m.c[1].x, m.c[1].y, m.c[1].z, x.y);
+  R[2 * N] = make_float4(m.c[2].x, m.c[2].y, m.c[2].z, x.z);
+  R[3 * N] = make_float4(xc.x, xc.y, xc.z, mass);
+  b.SpSelf[i] = make_float4(self.x, self.y, self.z, 0.f);
 }
 
 // velocityGradient (simkernels.js:224-245) over the neighbour list.
@@ -358,7 +399,7 @@ __device__ __forceinline__ bool sceneDone(const Bufs& b, uint32_t i) {
 //   fallback). With lambda0 = 0 both updates are the reference's.
 // flags & kMeasureOnly: residual only (the pass after the last iteration).
 template <bool kTrack>
-__global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4* __restrict__ velIn, int flags) {
+__global__ void XPBI_LB_SOLVEA k_solveA(Bufs b, int k, const float4* __restrict__ velIn, int flags) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
@@ -368,7 +409,7 @@ __global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4
   const bool warm0 = (flags & kWarm) != 0 && k == 0;
   const float4 pi = b.posS[i];
   const bool active = measure || (k < S.iterations && !sceneDone(b, i));
-  if (!active || waterW(pi.w)) {  // water: Sp is never read
+  if (!active || waterW(pi.w)) {  // water: its record is never read
     if (track) {
       b.rr[i] = 0.f;
       b.rc[i] = 0.f;
@@ -397,15 +438,19 @@ __global__ void __launch_bounds__(kThreads) k_solveA(Bufs b, int k, const float4
     if (k == 0) b.c0sq[i] = r0 * r0;
   }
   if (measure) return;
+  // an inactive constraint still takes part in the contact pass
+  const V3 xi = xyz(pi);
+  const V3 xci = xi + S.dt * xyz(velIn[i]);
+  const float mass = cx.mats[mi].mass;
   if (c.C == 0.f) {
     if (k == 0) b.lam[i] = lam0;
-    storeSp(b.Sp, i, mzero(), splat(0.f));
+    storeSp(b, i, mzero(), splat(0.f), xi, xci, mass);
     return;
   }
   const float dlam = S.omega * (-c.C - lamTerm - g * S.dt * c.cdot) / stiff;
   b.lam[i] = lam0 + dlam;
   const float imp = warm0 ? lam0 + dlam : dlam;
-  storeSp(b.Sp, i, mscale(c.GL, imp), c.sgrad * imp);
+  storeSp(b, i, mscale(c.GL, imp), c.sgrad * imp, xi, xci, mass);
 }
 
 // Network features of every slot at iteration 0 (zeros for water):
@@ -586,14 +631,14 @@ __device__ __forceinline__ V3 applyBoundary(const SceneDev& S, V3 xcIn, V3 vIn, 
 }
 
 struct SBData {
-  float4 p, v, s0, s1, s2;
+  float4 r0, r1, r2, r3;  // a neighbour's solveB record
 };
 
 // ---------------------------------------------------------------- solveB
 // Constraint dv gather + contact correction + boundaries (simkernels.js:315-366).
 // When a PBF pass follows, also stores the predicted position x + dt v_out
 // that pbfA / pbfB would otherwise recompute for every candidate.
-__global__ void __launch_bounds__(kThreads) k_solveB(Bufs b, int k, const float4* __restrict__ velIn,
+__global__ void XPBI_LB_SOLVEB k_solveB(Bufs b, int k, const float4* __restrict__ velIn,
                                                       float4* __restrict__ velOut, int writeXc) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
@@ -616,33 +661,59 @@ __global__ void __launch_bounds__(kThreads) k_solveB(Bufs b, int k, const float4
   const V3 xi = xyz(pi);
   V3 dv = splat(0.f), corr = splat(0.f);
   if (!waterW(pi.w)) {
-    const float4 s0 = Sp[3 * (size_t)i], s1 = Sp[3 * (size_t)i + 1], s2 = Sp[3 * (size_t)i + 2];
-    dv = v3(s0.w, s1.w, s2.w);
+    const size_t N = b.N;
+    dv = xyz(b.SpSelf[i]);
     const float Vi = vi4.w;
     const V3 xci = xi + S.dt * xyz(vi4);
     const float minD = S.minD;
     const float massI = m.mass;
-    forNbrs(b, cx, i, xi,
-            [&](uint32_t j) {
-              return SBData{ldg(posS + j), ldg(velIn + j), ldg(Sp + 3 * (size_t)j), ldg(Sp + 3 * (size_t)j + 1),
-                            ldg(Sp + 3 * (size_t)j + 2)};
-            },
-            [&](uint32_t, bool water, const SBData& d) {
-              if (water) return;
-              const V3 pb = xyz(d.p);
-              const M3 Sb = {{xyz(d.s0), xyz(d.s1), xyz(d.s2)}};
-              dv = dv + Vi * mul(Sb, gradWFast(S, pb - xi));
-              const V3 xcb = pb + S.dt * xyz(d.v);
-              const V3 dxc = xci - xcb;
-              const float d2 = dot(dxc, dxc);
-              if (d2 < minD * minD && d2 > 1e-18f) {
-                const float rinv = rsqrtf(d2);
-                const float dist = d2 * rinv;
-                const float mb = cx.mats[matOfW(d.p.w)].mass;
-                const float w = mb / (massI + mb);
-                corr = corr + dxc * (rinv * ((minD - dist) * w));
-              }
-            });
+    auto body = [&](bool water, const SBData& d) {
+      if (water) return;
+      const V3 pb = v3(d.r0.w, d.r1.w, d.r2.w);
+      const M3 Sb = {{xyz(d.r0), xyz(d.r1), xyz(d.r2)}};
+      dv = dv + Vi * mul(Sb, gradWFast(S, pb - xi));
+      const V3 dxc = xci - xyz(d.r3);
+      const float d2 = dot(dxc, dxc);
+      if (d2 < minD * minD && d2 > 1e-18f) {
+        const float rinv = rsqrtf(d2);
+        const float dist = d2 * rinv;
+        const float mb = d.r3.w;
+        const float w = mb / (massI + mb);
+        corr = corr + dxc * (rinv * ((minD - dist) * w));
+      }
+    };
+    const uint32_t cnt = b.nbrCount[i];
+    if (cnt != kNbrOverflow) {
+      // water neighbours are skipped before their record is loaded
+      forList<true>(listOf(b.nbr, i), cnt,
+                    [&](uint32_t e) {
+                      SBData d;
+                      if (e & kWaterBit) {
+                        d.r0 = d.r1 = d.r2 = d.r3 = make_float4(0.f, 0.f, 0.f, 0.f);
+                      } else {
+                        const float4* R = Sp + e;
+                        d.r0 = ldg(R);
+                        d.r1 = ldg(R + N);
+                        d.r2 = ldg(R + 2 * N);
+                        d.r3 = ldg(R + 3 * N);
+                      }
+                      return d;
+                    },
+                    [&](uint32_t, bool water, const SBData& d) { body(water, d); });
+    } else {
+      forRows(S, b.cellStart, xi, [&](uint32_t beg, uint32_t end) {
+#pragma unroll 1
+        for (uint32_t j = beg; j < end; ++j) {
+          if (j == i) continue;
+          const float4 pj = ldg(posS + j);
+          const V3 d = xi - xyz(pj);
+          if (dot(d, d) < S.support2 && !waterW(pj.w)) {
+            const float4* R = Sp + j;
+            body(false, SBData{ldg(R), ldg(R + N), ldg(R + 2 * N), ldg(R + 3 * N)});
+          }
+        }
+      });
+    }
   }
   V3 dvv = dv / (m.mass * S.dt);
   const float dvl = length(dvv);
@@ -665,7 +736,7 @@ __device__ __forceinline__ bool pbfActive(const SceneDev& S, int k) {
 // the current cell with predicted positions and records, in order, the
 // predicted neighbours of this pass: all of them for water, the water ones
 // for solids (the pairs pbfB uses, simkernels.js:457-458).
-__global__ void __launch_bounds__(kThreads) k_pbfA(Bufs b, int k) {
+__global__ void XPBI_LB_PBF k_pbfA(Bufs b, int k) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
@@ -750,7 +821,7 @@ struct PBData {
 // ---------------------------------------------------------------- pbfB
 // PBF position correction with s_corr (simkernels.js:441-477) over pbfA's
 // record of predicted neighbours.
-__global__ void __launch_bounds__(kThreads) k_pbfB(Bufs b, int k, const float4* __restrict__ velIn,
+__global__ void XPBI_LB_PBF k_pbfB(Bufs b, int k, const float4* __restrict__ velIn,
                                                     float4* __restrict__ velOut) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
@@ -803,7 +874,7 @@ __global__ void __launch_bounds__(kThreads) k_pbfB(Bufs b, int k, const float4* 
 
 // ---------------------------------------------------------------- xsph
 // simkernels.js:480-507
-__global__ void __launch_bounds__(kThreads) k_xsph(Bufs b, const float4* __restrict__ velIn,
+__global__ void XPBI_LB_UPDATE k_xsph(Bufs b, const float4* __restrict__ velIn,
                                                     float4* __restrict__ velOut) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
@@ -832,7 +903,7 @@ __global__ void __launch_bounds__(kThreads) k_xsph(Bufs b, const float4* __restr
 // Final F with return mapping (simkernels.js:510-525) fused with the CFL
 // clamp and position update (simkernels.js:528-542). Outputs go to the
 // "current" arrays, so neighbours still read the unclamped sorted inputs.
-__global__ void __launch_bounds__(kThreads) k_updateF_integrate(Bufs b, const float4* __restrict__ velIn) {
+__global__ void XPBI_LB_UPDATE k_updateF_integrate(Bufs b, const float4* __restrict__ velIn) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);

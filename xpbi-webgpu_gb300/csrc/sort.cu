@@ -278,7 +278,7 @@ void launch_scatter(const Bufs& b, cudaStream_t st) {
 }
 void launch_reorder(const Bufs& b, bool keepLam, cudaStream_t st) {
   // scratch for buckets too large for shared memory lives in the Sp buffer
-  // (12 floats per particle >= 2 words per particle), unused until solveA
+  // (16 floats per particle >= 2 words per particle), unused until solveA
   uint32_t* scratch = reinterpret_cast<uint32_t*>(b.Sp);
   k_bigcells<<<kBigGrid, kBigThreads, kSmemSortCap * sizeof(uint32_t), st>>>(b, scratch);
   k_reorder<<<grid(b.N, kThreads), kThreads, 0, st>>>(b, keepLam ? 1 : 0);

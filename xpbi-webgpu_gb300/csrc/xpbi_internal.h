@@ -90,7 +90,8 @@ struct Bufs {
   float* L;             // [9][N] kernel-gradient correction
   float* lam;           // [N] XPBI multiplier
   float* pbfLam;        // [N] PBF multiplier
-  float4* Sp;           // [3N] dlam * G L columns, self dv in .w
+  float4* Sp;           // [4][N] solveB neighbour record planes: dlam G L columns (x, y, z in .w), x + dt v, mass
+  float4* SpSelf;       // [N] own dv of the constraint update (sgrad * dlam)
   uint32_t* key;        // [N] global cell of each current particle
   uint32_t* tmp;        // [N] unordered cell-bucket fill
   uint32_t* sortedIdx;  // [N] global previous index of each sorted slot
