@@ -55,6 +55,31 @@ def test_dam_breach_small(xp, oracle, built_lib):
     compare(s1, ref, ref64, has_pbf=True)
 
 
+def test_dam_breach_fast_water(xp, oracle, built_lib):
+    """Water pushed to 12 m/s before the substep: the PBF passes pair
+    particles by predicted positions far from the current ones."""
+    sc = xp.scenes.config_dam_breach(scale=0.05)
+    p = xp.params_for(sc)
+    it = sc["iterations"]
+    with xp.Simulation(sc) as sim:
+        sim.write_params(p)
+        sim.step(10, it, True)
+        st = sim.read_state()
+        kinds = np.array([m["kind"] for m in sc["materials"]])
+        water = kinds[np.abs(st["pos"][:, 3]).astype(int)] == 6
+        vel = st["vel"].copy()
+        vel[water, 0] += 12.0
+        sim.write_state(0, vel=vel)
+        s0 = sim.read_state()
+        pw, mw = sim.uniforms()
+        ref = oracle.substep(pw, mw, s0, it, True, 4)
+        ref64 = oracle.substep(pw, mw, s0, it, True, 4, f64=True)
+        sim.encode_substep(it, True)
+        s1 = sim.read_state()
+    assert water.sum() > 0
+    compare(s1, ref, ref64, has_pbf=True)
+
+
 def test_reference_pbf_interleave(xp, oracle, built_lib):
     """pbfIterations unset: one PBF pass after every XPBI iteration."""
     sc = xp.scenes.config_dam_breach(scale=0.05)
@@ -139,4 +164,4 @@ def test_profile_substep_labels(xp, built_lib):
     lines = [l for l in text.splitlines() if l]
     assert len(lines) == n - 1  # the crowded-cell pass is timed with the reorder
     assert lines[0].startswith("count:") and lines[-1].startswith("updateF+integrate:")
-    assert sum(1 for l in lines if l.startswith("pbfB")) == 3
+    assert sum(1 for l in lines if l.startswith("pbfB:")) == 3
