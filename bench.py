@@ -34,15 +34,17 @@ UNIT = "particle-substeps/s"
 # Algorithmic bytes per particle for one launch of each kernel (compulsory
 # traffic, minimal layout), as (solid particle, water particle):
 #   solveA  solid: reads pos 16, vel 16, F 36, L 36, state 4, lambda 4, writes
-#           lambda 4, Sp 48 = 164; water: reads pos 16 and exits.
-#   solveB  solid: reads pos 16, vel 16, Sp 48, writes vel 16 = 96; water:
-#           pos, vel in, vel out = 48.
+#           lambda 4, the 64-byte neighbour record and the 16-byte own dv
+#           = 196; water: reads pos 16 and exits.
+#   solveB  solid: reads pos 16, vel 16, its record 64 and own dv 16 (every
+#           record is read by its neighbours; compulsory once), writes vel 16
+#           = 128; water: pos, vel in, vel out = 48.
 #   pbfA    pos 16, predicted position 16, writes the multiplier 4 = 36.
 #   pbfB    predicted position 16, multiplier 4, vel in 16, vel out 16 = 52.
 #   computeL pos 16, vel 16, writes L 36 = 68.   xsph pos, vel in, vel out = 48.
 #   updateF+integrate solid: reads pos 16, vel 16, F 36, L 36, state 4,
 #           writes pos 16, vel 16, F 36, state 4 = 180; water: no L = 144.
-ALGO_BYTES = {"solveA": (164, 16), "solveB": (96, 48), "pbfA": (36, 36), "pbfB": (52, 52),
+ALGO_BYTES = {"solveA": (196, 16), "solveB": (128, 48), "pbfA": (36, 36), "pbfB": (52, 52),
               "computeL": (68, 68), "xsph": (48, 48), "updateF+integrate": (180, 144),
               "reorder": (148, 148), "count": (20, 20), "fill": (8, 8), "scan": (8, 8)}
 
@@ -50,7 +52,7 @@ ALGO_BYTES = {"solveA": (164, 16), "solveB": (96, 48), "pbfA": (36, 36), "pbfB":
 # dram__bytes_write.sum over particles) from an ncu --set full capture of the
 # current kernels on the 1M-particle dam breach; the traffic of a launch grows
 # with the particle count, so the bench scales it by the workload's.
-NCU_TRAFFIC_PER_PARTICLE = {"solveB": 121.4, "solveA": 119.7, "pbfA": 101.8, "computeL": 229.5}
+NCU_TRAFFIC_PER_PARTICLE = {"solveB": 127.3, "solveA": 130.6, "pbfA": 101.8, "computeL": 229.5}
 
 
 def workload(name: str, rank: int = 0):
@@ -348,10 +350,10 @@ def run_xpbi(args, rank: int, world: int):
            "roofline": roofline, "clocks": clk, "gpu_launches": launches * args.steps,
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}}
     if rank == 0 and not args.no_cpu_baseline:
-        v, n, dt = cpu_baseline(args.cpu_scale, host_threads())
+        v, n, dt = cpu_baseline(args.cpu_scale, host_threads(), substeps=args.cpu_substeps)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": host_threads(), "kind": "port",
-                               "sample": f"f32 oracle port, one dam-breach substep (15 XPBI + 4 PBF "
-                                         f"iterations) of {n} particles, {dt:.1f} s"}
+                               "sample": f"f32 oracle port, {args.cpu_substeps} dam-breach substeps (15 XPBI + "
+                                         f"4 PBF iterations each) of {n} particles from rest, {dt:.1f} s"}
     if rank == 0:
         print(json.dumps(out))
     if dist:
@@ -366,6 +368,8 @@ def main():
     ap.add_argument("--impl", default="xpbi", choices=["xpbi", "reference"])
     ap.add_argument("--workload", default="dam_mix4")
     ap.add_argument("--cpu-scale", type=float, default=0.25)
+    ap.add_argument("--cpu-substeps", type=int, default=30,
+                    help="substeps of the CPU baseline sample (about 10 s on 16 cores)")
     ap.add_argument("--profile-substeps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--solver", default=None, choices=["learned", "plain"],

@@ -52,7 +52,12 @@ constexpr int kThreads = 128;
 #ifndef XPBI_MINB_SOLVEA
 #define XPBI_MINB_SOLVEA 7
 #endif
-#define XPBI_LB_SOLVEA __launch_bounds__(kThreads, XPBI_MINB_SOLVEA)
+// the tracked variant (residuals and the contact sum) carries more live
+// values through the loop; it gets its own bound
+#ifndef XPBI_MINB_SOLVEA_TRACK
+#define XPBI_MINB_SOLVEA_TRACK 6
+#endif
+#define XPBI_LB_SOLVEA __launch_bounds__(kThreads, kTrack ? XPBI_MINB_SOLVEA_TRACK : XPBI_MINB_SOLVEA)
 #ifdef XPBI_MINB_SOLVEB
 #define XPBI_LB_SOLVEB __launch_bounds__(kThreads, XPBI_MINB_SOLVEB)
 #else
