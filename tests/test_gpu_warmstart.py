@@ -85,11 +85,13 @@ def test_early_stop_skips_remaining_iterations(xp, built_lib):
     st = _rollout(xp, sc, 300)
     curves, _ = _curves(xp, sc, st, 0, substeps=2, tol=0.2)
     for r, used, c in curves:
-        assert 0 < used < sc["iterations"]
-        # the residuals that triggered the stop: constraint and contact
-        assert r[1 + used] <= 0.2 * 1.0001 and c[1 + used] <= 0.2 * 1.0001
-        assert r[used] > 0.2 or c[used] > 0.2  # and not one iteration earlier
-        assert np.isnan(r[2 + used:-1]).all()
+        # a stop found at iteration k (residuals of the state entering it)
+        # takes effect after iteration k's update: k + 1 iterations applied
+        assert 1 < used < sc["iterations"]
+        k = used - 1
+        assert r[1 + k] <= 0.2 * 1.0001 and c[1 + k] <= 0.2 * 1.0001  # constraint and contact
+        assert r[k] > 0.2 or c[k] > 0.2  # and not one iteration earlier
+        assert np.isnan(r[1 + used:-1]).all()  # iterations after the stop did not run
 
 
 def test_network_warm_start_gains(xp, tw):

@@ -420,12 +420,12 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
   for (int k = 0; k < sch.K; ++k) {
     launch_solveA(b, k, b.velS[in], aflags, st);
     R.mark(st, "solveA");
+    launch_solveB(b, k, b.velS[in], b.velS[in ^ 1], sch.pbf[k] != 0, sch.reduce ? kTrackResid : 0, st);
+    R.mark(st, "solveB");
     if (sch.reduce) {
       launch_resid_reduce(b, k, (aflags & kWarm) != 0, st);
       R.mark(st, "residual");
     }
-    launch_solveB(b, k, b.velS[in], b.velS[in ^ 1], sch.pbf[k] != 0, st);
-    R.mark(st, "solveB");
     in ^= 1;
     if (sch.pbf[k]) {
       launch_pbfA(b, k, b.velS[in], st);
@@ -438,6 +438,8 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
   if (sch.track) {  // residual of the state the iterations leave behind
     launch_solveA(b, sch.K, b.velS[in], kTrackResid | kMeasureOnly, st);
     R.mark(st, "solveA(measure)");
+    launch_solveB(b, sch.K, b.velS[in], nullptr, false, kTrackResid | kMeasureOnly, st);
+    R.mark(st, "solveB(measure)");
     launch_resid_reduce(b, -1, false, st);
     R.mark(st, "residual");
   }
@@ -458,7 +460,7 @@ int kernelsPerSubstep(const Schedule& sch) {
   if (sch.features) n += 1;
   if (sch.mode == 1) n += 2;
   if (sch.mode == 2) n += 1;
-  if (sch.track) n += 3;
+  if (sch.track) n += 4;
   if (sch.keepLam) n += 1;
   return n;
 }
@@ -1021,7 +1023,7 @@ int xpbi_read_residuals(xpbi_sim* sim, uint32_t scene, double* norms, int32_t ca
     // [ |C(v_pred)|, |r_0| .. |r_{K-1}|, |r| after the last applied iteration ]
     std::vector<double> out;
     out.push_back(std::sqrt(c0));
-    for (int k = 0; k < K && k < kMaxResid - 1; ++k) out.push_back(k < used + 1 ? std::sqrt(r[k]) : NAN);
+    for (int k = 0; k < K && k < kMaxResid - 1; ++k) out.push_back(k < used ? std::sqrt(r[k]) : NAN);
     out.push_back(std::sqrt(r[kMaxResid - 1]));
     for (int q = 0; q < cap && q < (int)out.size(); ++q) norms[q] = out[q];
   }
@@ -1044,7 +1046,7 @@ int xpbi_read_contact_residuals(xpbi_sim* sim, uint32_t scene, double* norms, in
     // same slots as xpbi_read_residuals; slot 0 repeats iteration 0's value
     std::vector<double> out;
     out.push_back(std::sqrt(c0));
-    for (int k = 0; k < K && k < kMaxResid - 1; ++k) out.push_back(k < used + 1 ? std::sqrt(r[k]) : NAN);
+    for (int k = 0; k < K && k < kMaxResid - 1; ++k) out.push_back(k < used ? std::sqrt(r[k]) : NAN);
     out.push_back(std::sqrt(r[kMaxResid - 1]));
     for (int q = 0; q < cap && q < (int)out.size(); ++q) norms[q] = out[q];
   }

@@ -52,10 +52,9 @@ constexpr int kThreads = 128;
 #ifndef XPBI_MINB_SOLVEA
 #define XPBI_MINB_SOLVEA 7
 #endif
-// the tracked variant (residuals and the contact sum) carries more live
-// values through the loop; it gets its own bound
+// the tracked variant (residual stores) has its own override
 #ifndef XPBI_MINB_SOLVEA_TRACK
-#define XPBI_MINB_SOLVEA_TRACK 6
+#define XPBI_MINB_SOLVEA_TRACK 7
 #endif
 #define XPBI_LB_SOLVEA __launch_bounds__(kThreads, kTrack ? XPBI_MINB_SOLVEA_TRACK : XPBI_MINB_SOLVEA)
 #ifdef XPBI_MINB_SOLVEB
@@ -296,12 +295,8 @@ struct Constraint {
   V3 sgrad;       // self gradient (per unit multiplier)
   V3 logSigTr;    // log of the trial singular values (clamped like safeSig)
   float nNbr;     // solid neighbours in the sweep
-  float contact2; // |contact correction|^2 solveB would apply at these velocities (kContact only)
 };
 
-// kContact: also form the contact position correction of the same state
-// (the sum solveB applies, simkernels.js:340-356) for the contact residual.
-template <bool kContact = false>
 __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& cx, uint32_t i, float4 pi,
                                                      const float4* __restrict__ velIn, const MatDev& m, float st) {
   const SceneDev& S = *cx.scene;
@@ -312,9 +307,6 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
   M3 G = mzero();
   V3 sv = splat(0.f);
   float q00 = 0.f, q11 = 0.f, q22 = 0.f, q01 = 0.f, q02 = 0.f, q12 = 0.f, cnt = 0.f;
-  V3 corr = splat(0.f);
-  const V3 xci = xi + S.dt * vi;
-  const float massI = cx.mats[matOfW(pi.w)].mass;
   forNbrs(b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
           [&](uint32_t, bool water, const PV& d) {
             if (water) return;
@@ -323,16 +315,7 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
             const V3 dv = (xyz(d.v) - vi) * Vb;
             G = madd(G, M3{{dv * gt.x, dv * gt.y, dv * gt.z}});
             sv = sv + gt * Vb;
-            const float mb = cx.mats[matOfW(d.p.w)].mass;
-            if (kContact) {
-              const V3 dxc = xci - (xyz(d.p) + S.dt * xyz(d.v));
-              const float d2 = dot(dxc, dxc);
-              if (d2 < S.minD * S.minD && d2 > 1e-18f) {
-                const float rinv = rsqrtf(d2);
-                corr = corr + dxc * (rinv * ((S.minD - d2 * rinv) * (mb / (massI + mb))));
-              }
-            }
-            const float c = Vb * Vb / mb;
+            const float c = Vb * Vb / cx.mats[matOfW(d.p.w)].mass;
             const V3 cg = gt * c;
             q00 += cg.x * gt.x;
             q11 += cg.y * gt.y;
@@ -344,7 +327,6 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
           });
   Constraint out;
   out.nNbr = cnt;
-  out.contact2 = dot(corr, corr);
   const M3 Fn = loadM(b.FS, b.N, i);
   const M3 Ftr = mul(madd(mident(), mscale(G, S.dt)), Fn);
   const SVD sd = svd3Fast(Ftr);
@@ -387,10 +369,8 @@ __device__ __forceinline__ bool sceneDone(const Bufs& b, uint32_t i) {
 //   damped update drives to zero; without the damping term the Jacobi fixed
 //   point sits at C + alphaT lambda = -gamma dt cdot, not 0), 0 for an
 //   inactive constraint (C = 0), and at iteration 0 the residual at
-//   lambda = 0 to c0sq; also |contact correction|^2 of the same state to rc
-//   (the contact constraints the iteration solves beside the multipliers).
-//   The tracked variant is a separate instantiation (kTrack) so the plain
-//   path carries none of it.
+//   lambda = 0 to c0sq. The tracked variant is a separate instantiation
+//   (kTrack) so the plain path carries none of it.
 // flags & kWarm (iteration 0): starts from lambda0 = lamWarm instead of 0.
 //   Its impulse has not been applied to the velocities this pass sees, so the
 //   first correction uses the linearised post-impulse residual: applying
@@ -417,7 +397,6 @@ __global__ void XPBI_LB_SOLVEA k_solveA(Bufs b, int k, const float4* __restrict_
   if (!active || waterW(pi.w)) {  // water: its record is never read
     if (track) {
       b.rr[i] = 0.f;
-      b.rc[i] = 0.f;
       if (k == 0) b.c0sq[i] = 0.f;
     }
     return;
@@ -425,7 +404,7 @@ __global__ void XPBI_LB_SOLVEA k_solveA(Bufs b, int k, const float4* __restrict_
   const uint32_t mi = matOfW(pi.w);
   const float st = b.stateS[i];
   const MatDev m = hardenedMat(cx.mats[mi], st);
-  const Constraint c = evalConstraint<kTrack>(b, cx, i, pi, velIn, m, st);
+  const Constraint c = evalConstraint(b, cx, i, pi, velIn, m, st);
   const float g = S.kDamp;
   const float stiff = (1.f + g) * c.denom + S.alphaT;  // d(residual) / d(applied multiplier)
   const float r0 = c.C + g * S.dt * c.cdot;            // residual at lambda = 0
@@ -439,7 +418,6 @@ __global__ void XPBI_LB_SOLVEA k_solveA(Bufs b, int k, const float4* __restrict_
     // there would add a term no iteration can change
     const float r = c.C == 0.f ? 0.f : r0 + lamTerm;
     b.rr[i] = r * r;
-    b.rc[i] = c.contact2;
     if (k == 0) b.c0sq[i] = r0 * r0;
   }
   if (measure) return;
@@ -521,55 +499,76 @@ __global__ void k_warm_from_prev(Bufs b) {
 // scene s in a fixed order; k_resid_final adds the chunks in order.
 // Sums: constraint residual^2, (iteration 0) residual^2 at lambda = 0,
 // contact correction^2.
+// Chunk sums are formed in f32 (a convergence test on sums of squares needs
+// nothing finer, and f64 is slow here) by a fixed warp butterfly and a fixed
+// combine of the 8 warps; the chunks are added in f64.
 constexpr int kResidSums = 3;
 __global__ void __launch_bounds__(256) k_resid_partial(Bufs b, int k) {
-  __shared__ double red[kResidSums][256];
+  __shared__ float red[kResidSums][8];
   const uint32_t s = blockIdx.y, c = blockIdx.x;
   const SceneDev& S = b.scenes[s];
   const uint32_t n = S.n, base = S.pBase;
   const uint32_t lo = base + (uint32_t)(((uint64_t)n * c) / kResidChunks);
   const uint32_t hi = base + (uint32_t)(((uint64_t)n * (c + 1)) / kResidChunks);
-  double a = 0.0, a0 = 0.0, ac = 0.0;
+  float a = 0.f, a0 = 0.f, ac = 0.f;
   if (!b.done[s] || k < 0) {
     for (uint32_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
-      a += (double)b.rr[p];
-      ac += (double)b.rc[p];
-      if (k == 0) a0 += (double)b.c0sq[p];
+      a += b.rr[p];
+      ac += b.rc[p];
+      if (k == 0) a0 += b.c0sq[p];
     }
   }
-  red[0][threadIdx.x] = a;
-  red[1][threadIdx.x] = a0;
-  red[2][threadIdx.x] = ac;
-  __syncthreads();
-  for (int w = 128; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) {
 #pragma unroll
-      for (int q = 0; q < kResidSums; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + w];
-    }
-    __syncthreads();
+  for (int off = 16; off > 0; off >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, off);
+    a0 += __shfl_xor_sync(0xffffffffu, a0, off);
+    ac += __shfl_xor_sync(0xffffffffu, ac, off);
   }
-  if (threadIdx.x < kResidSums) b.residPart[(s * kResidChunks + c) * kResidSums + threadIdx.x] = red[threadIdx.x][0];
+  const uint32_t w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31u) == 0) {
+    red[0][w] = a;
+    red[1][w] = a0;
+    red[2][w] = ac;
+  }
+  __syncthreads();
+  if (threadIdx.x < kResidSums) {
+    double t = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) t += (double)red[threadIdx.x][q];
+    b.residPart[(s * kResidChunks + c) * kResidSums + threadIdx.x] = t;
+  }
 }
 
-// k >= 0: iteration k's residuals (early stop); k < 0: after the last
-// iteration (slot kMaxResid - 1). A scene stops once both its constraint
-// residual and its contact residual are within tol of their values entering
-// iteration 0 (an early stop also ends the contact passes, which the
-// constraint residual does not see). With a warm start, iteration 0's
-// constraint residual is the linearised estimate before the warm impulse is
-// applied, so the earliest stop is after iteration 0.
+// k >= 0: the residuals of the state entering iteration k (early stop),
+// reduced after iteration k's update; k < 0: after the last iteration (slot
+// kMaxResid - 1). A scene stops, skipping iterations k+1.., once both its
+// constraint residual and its contact residual are within tol of their
+// values entering iteration 0 (an early stop also ends the contact passes,
+// which the constraint residual does not see). With a warm start, iteration
+// 0's constraint residual is the linearised estimate before the warm impulse
+// is applied, so it never stops the solve.
+// One warp per scene: lane l adds chunks l, l + 32, ... in order, then a
+// fixed butterfly combines the lanes, so the sums do not depend on timing.
 __global__ void k_resid_final(Bufs b, int k, int warm) {
-  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= b.S) return;
+  const uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31u;
+  if (s >= b.S) return;  // whole warps leave together
   const SceneDev& S = b.scenes[s];
   if (k >= 0 && (b.done[s] || k >= S.iterations)) return;
   double a = 0.0, a0 = 0.0, ac = 0.0;
-  for (int c = 0; c < kResidChunks; ++c) {
+  for (int c = (int)lane; c < kResidChunks; c += 32) {
     const double* part = b.residPart + (s * kResidChunks + c) * kResidSums;
     a += part[0];
     a0 += part[1];
     ac += part[2];
   }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, off);
+    a0 += __shfl_xor_sync(0xffffffffu, a0, off);
+    ac += __shfl_xor_sync(0xffffffffu, ac, off);
+  }
+  if (lane != 0) return;
   if (k < 0) {
     b.resid[(size_t)s * kMaxResid + (kMaxResid - 1)] = a;
     b.residC[(size_t)s * kMaxResid + (kMaxResid - 1)] = ac;
@@ -584,12 +583,8 @@ __global__ void k_resid_final(Bufs b, int k, int warm) {
     b.cc0[s] = ac;
   }
   const double tol = (double)S.residTol, tolC = (double)S.residTolC;
-  if (tol > 0.0 && a <= tol * tol * b.c0[s] && ac <= tolC * tolC * b.cc0[s] && !(warm && k == 0)) {
-    b.done[s] = 1;
-    b.itersUsed[s] = k;
-  } else {
-    b.itersUsed[s] = k + 1;
-  }
+  if (tol > 0.0 && a <= tol * tol * b.c0[s] && ac <= tolC * tolC * b.cc0[s] && !(warm && k == 0)) b.done[s] = 1;
+  b.itersUsed[s] = k + 1;
 }
 
 // keep this substep's final multipliers for the next substep's features
@@ -643,8 +638,12 @@ struct SBData {
 // Constraint dv gather + contact correction + boundaries (simkernels.js:315-366).
 // When a PBF pass follows, also stores the predicted position x + dt v_out
 // that pbfA / pbfB would otherwise recompute for every candidate.
+// flags & kTrackResid: writes |contact correction|^2 of the velocities
+//   entering this iteration to rc (the contact residual; 0 for water).
+// flags & kMeasureOnly: the contact residual only, of every solid slot, no
+//   velocity update (the pass after the last iteration).
 __global__ void XPBI_LB_SOLVEB k_solveB(Bufs b, int k, const float4* __restrict__ velIn,
-                                                      float4* __restrict__ velOut, int writeXc) {
+                                                      float4* __restrict__ velOut, int writeXc, int flags) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
@@ -653,7 +652,9 @@ __global__ void XPBI_LB_SOLVEB k_solveB(Bufs b, int k, const float4* __restrict_
   const float4* __restrict__ Sp = b.Sp;
   const float4 vi4 = velIn[i];
   const float4 pi = posS[i];
-  if (k >= S.iterations || sceneDone(b, i)) {
+  const bool track = (flags & kTrackResid) != 0;
+  const bool measure = (flags & kMeasureOnly) != 0;
+  if (!measure && (k >= S.iterations || sceneDone(b, i))) {
     velOut[i] = vi4;
     if (writeXc) {
       const V3 xc = xyz(pi) + S.dt * xyz(vi4);
@@ -720,6 +721,8 @@ __global__ void XPBI_LB_SOLVEB k_solveB(Bufs b, int k, const float4* __restrict_
       });
     }
   }
+  if (track) b.rc[i] = dot(corr, corr);
+  if (measure) return;
   V3 dvv = dv / (m.mass * S.dt);
   const float dvl = length(dvv);
   if (dvl > S.dvCap) dvv = dvv * (S.dvCap / dvl);
@@ -956,11 +959,12 @@ void launch_warm_from_net(const Bufs& b, cudaStream_t st) { k_warm_from_net<<<gr
 void launch_warm_from_prev(const Bufs& b, cudaStream_t st) { k_warm_from_prev<<<grid(b.N), kThreads, 0, st>>>(b); }
 void launch_resid_reduce(const Bufs& b, int k, bool warm, cudaStream_t st) {
   k_resid_partial<<<dim3(kResidChunks, b.S), 256, 0, st>>>(b, k);
-  k_resid_final<<<(b.S + 127) / 128, 128, 0, st>>>(b, k, warm ? 1 : 0);
+  k_resid_final<<<(b.S + 3) / 4, 128, 0, st>>>(b, k, warm ? 1 : 0);
 }
 void launch_keep_lambda(const Bufs& b, cudaStream_t st) { k_keep_lambda<<<grid(b.N), kThreads, 0, st>>>(b); }
-void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, cudaStream_t st) {
-  k_solveB<<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, writeXc ? 1 : 0);
+void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, int flags,
+                   cudaStream_t st) {
+  k_solveB<<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, writeXc ? 1 : 0, flags);
 }
 void launch_pbfA(const Bufs& b, int k, const float4* velIn, cudaStream_t st) {
   (void)velIn;  // predicted positions were stored by the preceding solveB

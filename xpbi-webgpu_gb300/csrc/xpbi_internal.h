@@ -11,7 +11,7 @@ constexpr uint32_t kKindSnow = 5u;
 constexpr uint32_t kKindWater = 6u;
 
 constexpr uint32_t kNbrCap = 64u;      // neighbour-list capacity per particle
-constexpr int kResidChunks = 64;       // per-scene partial sums of the residual
+constexpr int kResidChunks = 512;      // per-scene partial sums of the residual
 constexpr int kMaxResid = 129;         // residual slots per scene (iterations + 1)
 constexpr int kFeat = 16;              // network features per particle
 
@@ -154,7 +154,8 @@ void mlp_pack(const float* dParams, void* dBlob, cudaStream_t st);
 // skipZero: tiles whose 128 feature rows are all zero output 0 without running the network
 cudaError_t mlp_forward(const float* dX, uint32_t rows, const void* dBlob, float* dY, float* dZ, int* dErr,
                         cudaStream_t st, bool skipZero = false);
-void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, cudaStream_t st);
+void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, int flags,
+                   cudaStream_t st);
 void launch_pbfA(const Bufs& b, int k, const float4* velIn, cudaStream_t st);
 void launch_pbfB(const Bufs& b, int k, const float4* velIn, float4* velOut, cudaStream_t st);
 void launch_xsph(const Bufs& b, const float4* velIn, float4* velOut, cudaStream_t st);
