@@ -259,16 +259,16 @@ __device__ __forceinline__ M3 velocityGradient(const Bufs& b, const Ctx& cx, uin
                                                const float4* __restrict__ velIn) {
   const SceneDev& S = *cx.scene;
   const float4* __restrict__ posS = b.posS;
-  const M3 Li = loadM(b.L, b.N, i);
-  M3 G = mzero();
+  // sum dv_b (L g_b)^T = (sum dv_b g_b^T) L^T: L applied once, after the loop
+  M3 A = mzero();
   forNbrs(b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
           [&](uint32_t, bool water, const PV& d) {
             if (water) return;
-            const V3 gt = mul(Li, gradWFast(S, xi - xyz(d.p)));
+            const V3 g = gradWFast(S, xi - xyz(d.p));
             const V3 dv = (xyz(d.v) - vi) * d.v.w;
-            G = madd(G, M3{{dv * gt.x, dv * gt.y, dv * gt.z}});
+            A = madd(A, M3{{dv * g.x, dv * g.y, dv * g.z}});
           });
-  return G;
+  return mul(A, transpose(loadM(b.L, b.N, i)));
 }
 
 // ---------------------------------------------------------------- solveA
@@ -303,28 +303,39 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
   const float4* __restrict__ posS = b.posS;
   const V3 xi = xyz(pi);
   const V3 vi = xyz(velIn[i]);
-  const M3 Li = loadM(b.L, b.N, i);
-  M3 G = mzero();
-  V3 sv = splat(0.f);
-  float q00 = 0.f, q11 = 0.f, q22 = 0.f, q01 = 0.f, q02 = 0.f, q12 = 0.f, cnt = 0.f;
+  // The sums run over the raw kernel gradients g_b; the correction L is
+  // applied once afterwards: with gt_b = L g_b,
+  //   G = sum dv_b gt_b^T = A L^T,  s = L sum V_b g_b,  Q = L P L^T,
+  // A = sum dv_b g_b^T, P = sum (V_b^2 / m_b) g_b g_b^T (same terms, the L
+  // products factored out of the pair loop).
+  M3 A = mzero();
+  V3 sg = splat(0.f);
+  float p00 = 0.f, p11 = 0.f, p22 = 0.f, p01 = 0.f, p02 = 0.f, p12 = 0.f, cnt = 0.f;
   forNbrs(b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
           [&](uint32_t, bool water, const PV& d) {
             if (water) return;
-            const V3 gt = mul(Li, gradWFast(S, xi - xyz(d.p)));
+            const V3 g = gradWFast(S, xi - xyz(d.p));
             const float Vb = d.v.w;
             const V3 dv = (xyz(d.v) - vi) * Vb;
-            G = madd(G, M3{{dv * gt.x, dv * gt.y, dv * gt.z}});
-            sv = sv + gt * Vb;
+            A = madd(A, M3{{dv * g.x, dv * g.y, dv * g.z}});
+            sg = sg + g * Vb;
             const float c = Vb * Vb / cx.mats[matOfW(d.p.w)].mass;
-            const V3 cg = gt * c;
-            q00 += cg.x * gt.x;
-            q11 += cg.y * gt.y;
-            q22 += cg.z * gt.z;
-            q01 += cg.x * gt.y;
-            q02 += cg.x * gt.z;
-            q12 += cg.y * gt.z;
+            const V3 cg = g * c;
+            p00 += cg.x * g.x;
+            p11 += cg.y * g.y;
+            p22 += cg.z * g.z;
+            p01 += cg.x * g.y;
+            p02 += cg.x * g.z;
+            p12 += cg.y * g.z;
             cnt += 1.f;
           });
+  const M3 Li = loadM(b.L, b.N, i);
+  const M3 LiT = transpose(Li);
+  const M3 G = mul(A, LiT);
+  const V3 sv = mul(Li, sg);
+  const M3 Qm = mul(mul(Li, M3{{v3(p00, p01, p02), v3(p01, p11, p12), v3(p02, p12, p22)}}), LiT);
+  const float q00 = Qm.c[0].x, q11 = Qm.c[1].y, q22 = Qm.c[2].z;
+  const float q01 = Qm.c[1].x, q02 = Qm.c[2].x, q12 = Qm.c[2].y;
   Constraint out;
   out.nNbr = cnt;
   const M3 Fn = loadM(b.FS, b.N, i);
