@@ -233,6 +233,7 @@ void buildSceneDev(const SceneHost& s, uint32_t sceneIdx, SceneDev& d, MatDev* m
     M.p3 = wf(q, 7);
     M.boundFriction = wf(q, 12);
     M.mass = wf(q, 13);
+    M.massPerDensity = M.density != 0.f ? M.mass / M.density : 0.f;
   }
 }
 

@@ -868,7 +868,7 @@ __global__ void XPBI_LB_PBF k_pbfB(Bufs b, int k, const float4* __restrict__ vel
     const float x = poly6Fast(S, r2) * S.invW0;
     const float x2 = x * x;
     const float sCorr = -S.sCorrK * (x2 * x2);
-    dp = dp + (li + d.lb + sCorr) * spikyGradFast(S, dxv, r2) * (mw.mass / mw.density);
+    dp = dp + (li + d.lb + sCorr) * spikyGradFast(S, dxv, r2) * mw.massPerDensity;
   };
   const uint32_t cnt = b.nbrPCount[i];
   if (cnt != kNbrOverflow) {

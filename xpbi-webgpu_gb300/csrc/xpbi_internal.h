@@ -72,7 +72,8 @@ struct MatDev {
   uint32_t kind;
   float p0, p1, p2, p3;
   float boundFriction, mass;
-  float pad[2];
+  float massPerDensity;     // mass / density (host f32, the same IEEE quotient as on the device)
+  float pad;
 };
 
 // Device buffers of one handle. "Current" arrays hold the state between
