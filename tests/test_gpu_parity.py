@@ -7,7 +7,7 @@ particle state within 1e-4 normwise relative error (parity_util.REL_TOL).
 import numpy as np
 import pytest
 
-from parity_util import REL_TOL, compare, rel, run_pair
+from parity_util import REL_TOL, compare, perturbed_runs, rel, run_pair
 
 pytestmark = pytest.mark.gpu
 
@@ -20,7 +20,7 @@ def _scene(xp, name, **kw):
 def test_sand_column_config(xp, oracle, built_lib, warm):
     sc = xp.scenes.config_sand_column()
     s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=warm)
-    rep = compare(s1, ref, ref64)
+    rep = compare(s1, ref, ref64, perturbed=perturbed_runs(oracle, sc, s0, xp=xp))
     print("sand_column", warm, rep)
 
 
@@ -30,7 +30,7 @@ def test_sand_column_after_collapse_starts(xp, oracle, built_lib):
     # reaches the floor after ~160 substeps; by 300 it is flowing
     s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=300)
     assert np.abs(ref["aux"][:, 1]).max() > 0
-    compare(s1, ref, ref64)
+    compare(s1, ref, ref64, perturbed=perturbed_runs(oracle, sc, s0, xp=xp))
 
 
 @pytest.mark.parametrize("name", ["sand_column", "sand_two_blocks", "snowball_smash", "plasticine",
@@ -38,7 +38,7 @@ def test_sand_column_after_collapse_starts(xp, oracle, built_lib):
 def test_reference_demo_scenes(xp, oracle, built_lib, name):
     sc = _scene(xp, name)
     s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=12)
-    rep = compare(s1, ref, ref64, has_pbf=sc["hasWater"])
+    rep = compare(s1, ref, ref64, has_pbf=sc["hasWater"], perturbed=perturbed_runs(oracle, sc, s0, xp=xp))
     print(name, len(sc["positions"]), rep)
 
 
@@ -46,13 +46,13 @@ def test_nacc_snowball_wall_impact(xp, oracle, built_lib):
     sc = xp.scenes.config_nacc_snowball()
     # ~120 substeps until the sphere reaches the wall; start near impact
     s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=125)
-    compare(s1, ref, ref64)
+    compare(s1, ref, ref64, perturbed=perturbed_runs(oracle, sc, s0, xp=xp))
 
 
 def test_dam_breach_small(xp, oracle, built_lib):
     sc = xp.scenes.config_dam_breach(scale=0.05)
     s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=10)
-    compare(s1, ref, ref64, has_pbf=True)
+    compare(s1, ref, ref64, has_pbf=True, perturbed=perturbed_runs(oracle, sc, s0, xp=xp))
 
 
 def test_dam_breach_fast_water(xp, oracle, built_lib):
@@ -85,7 +85,7 @@ def test_reference_pbf_interleave(xp, oracle, built_lib):
     sc = xp.scenes.config_dam_breach(scale=0.05)
     p = xp.params_for(sc, pbfIterations=None)
     s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=3, params=p)
-    compare(s1, ref, ref64, has_pbf=True)
+    compare(s1, ref, ref64, has_pbf=True, perturbed=perturbed_runs(oracle, sc, s0, params=p, xp=xp))
 
 
 def test_collider_active(xp, oracle, built_lib):
@@ -93,13 +93,13 @@ def test_collider_active(xp, oracle, built_lib):
     p = xp.params_for(sc, colliderActive=True, colliderPos=[0.5, 0.45, 0.5], colliderR=0.08,
                       colliderVel=[0.3, -0.5, 0.0])
     s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=4, params=p)
-    compare(s1, ref, ref64)
+    compare(s1, ref, ref64, perturbed=perturbed_runs(oracle, sc, s0, params=p, xp=xp))
 
 
 def test_zero_iterations(xp, oracle, built_lib):
     sc = xp.scenes.elastic_block()
     s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=2, iterations=0)
-    compare(s1, ref, ref64)
+    compare(s1, ref, ref64, perturbed=perturbed_runs(oracle, sc, s0, iterations=0, xp=xp))
 
 
 def test_graph_step_matches_encode(xp, built_lib):
