@@ -178,6 +178,23 @@ def make_sim(xp, scenes, stream, preroll: int):
     return sim, has_water
 
 
+def max_over_ranks(x: float, dist, device: str = "cuda") -> float:
+    """The job's time is its slowest rank's: all-reduce MAX (NCCL tensors
+    live on the GPU, gloo ones on the host)."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(particles_per_rank: int, world: int, steps: int, seconds: float) -> float:
+    """Whole-job particle-substeps/s: every rank's particles over the slowest
+    rank's time (weak scaling: each rank steps its own scenes)."""
+    return particles_per_rank * world * steps / seconds
+
+
 def timed_steps(sim, has_water, steps, stream, dist):
     import torch
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -190,11 +207,7 @@ def timed_steps(sim, has_water, steps, stream, dist):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     sim.synchronize()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    return ms
+    return max_over_ranks(ms, dist)
 
 
 def residual_stats(sim, has_water, n_scenes, substeps):
@@ -238,7 +251,7 @@ def run_xpbi(args, rank: int, world: int):
     clocks.start()
     ms_plain = timed_steps(sim, has_water, args.steps, stream, dist)
     clk = clocks.stop()
-    value_plain = n_total * world * args.steps / (ms_plain / 1e3)
+    value_plain = job_throughput(n_total, world, args.steps, ms_plain / 1e3)
     launches = sim.launches_per_substep(-1, has_water)
     solvers = {"plain": {"value": value_plain, "ms_per_step": ms_plain / args.steps,
                          "iterations": [s["iterations"] for s in scenes][:4]}}
@@ -263,7 +276,7 @@ def run_xpbi(args, rank: int, world: int):
         clocks.start()
         ms = timed_steps(sim, has_water, args.steps, stream, dist)
         clk = clocks.stop()
-        value = n_total * world * args.steps / (ms / 1e3)
+        value = job_throughput(n_total, world, args.steps, ms / 1e3)
         launches = sim.launches_per_substep(-1, has_water)
         sim.set_solver(1, tau, True, False, contact_rel_tol=tau_c)
         rel_l, relc_l, used_l = residual_stats(sim, has_water, len(scenes), args.residual_substeps)
@@ -294,12 +307,8 @@ def run_xpbi(args, rank: int, world: int):
         for k in range(len(scenes)):
             sim.read_pos(k, out=pinned[k])
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = n_total * world * args.steps / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
+    e2e = job_throughput(n_total, world, args.steps, e2e_s)
     # uniforms uploaded per step: SceneDev (192 B) + MatDev table (8 x 48 B)
     # + packed material words (8 x 64 B) per scene
     h2d = len(scenes) * (192 + 8 * 48 + 8 * 64)
