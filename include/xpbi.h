@@ -184,6 +184,26 @@ int xpbi_device_ptrs(xpbi_sim* sim, void** pos4, void** vel4, void** materials);
 /* Number of kernel launches one substep issues with this schedule. */
 int xpbi_launches_per_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t* out);
 
+/* ---- autotuner (no counterpart in the reference) ----
+ * solveA and solveB are built in several register-allocation variants
+ * (resident blocks per SM traded against registers). xpbi_autotune runs the
+ * substep's preparation (sort, reorder, Bonet-Lok correction) on the current
+ * state and times iteration 0 of every variant `repeats` times on this
+ * handle's own data, then keeps the fastest of each for the handle (the
+ * default on a tie within 1%). Everything xpbi_read_state reports is left
+ * as it was (the working buffers it overwrites are saved and restored); it
+ * synchronises the handle's stream and allocates temporary device memory. chosen[2] (may be NULL)
+ * receives the variant indices, ms (may be NULL) the mean time of each
+ * variant: XPBI_SOLVEA_VARIANTS entries for solveA, then solveB's. All
+ * variants compute the same results; only their speed differs. */
+#define XPBI_SOLVEA_VARIANTS 4
+#define XPBI_SOLVEB_VARIANTS 3
+int xpbi_autotune(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t repeats, int32_t* chosen, float* ms,
+                  int32_t cap);
+
+/* Select variants directly (-1 keeps the current one); 0 is the default. */
+int xpbi_set_variants(xpbi_sim* sim, int32_t solve_a, int32_t solve_b);
+
 /* ---- solver modes (no counterpart in the reference) ----
  * mode 0: the reference solve (every XPBI iteration starts from lambda = 0).
  * mode 1: iteration 0 starts from the particle's previous-substep multiplier

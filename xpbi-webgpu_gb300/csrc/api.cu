@@ -281,6 +281,8 @@ struct xpbi_sim {
   bool netLoaded = false;
   float* netParams = nullptr;
   int* netErr = nullptr;
+  // register-allocation variants of solveA / solveB (xpbi_autotune)
+  int tuneA = 0, tuneB = 0;
 };
 
 namespace {
@@ -341,11 +343,12 @@ struct Schedule {
   bool reduce = false;   // per-iteration residual reductions (history or early stop)
   bool features = false; // network features at iteration 0
   bool keepLam = false;  // carry the final multipliers into the next substep
+  int varA = 0, varB = 0; // solveA / solveB variants
   std::string key() const {
     std::string k = std::to_string(K) + ":";
     for (char c : pbf) k += c ? '1' : '0';
     k += ":" + std::to_string(mode) + (track ? "t" : "") + (reduce ? "r" : "") + (features ? "f" : "") +
-         (keepLam ? "l" : "");
+         (keepLam ? "l" : "") + ":v" + std::to_string(varA) + std::to_string(varB);
     return k;
   }
 };
@@ -357,6 +360,8 @@ Schedule schedule(const xpbi_sim* s) {
   sch.reduce = s->track || s->residTol > 0.f;
   sch.features = s->features || s->mode == 1;
   sch.keepLam = s->mode != 0 || sch.features;
+  sch.varA = s->tuneA;
+  sch.varB = s->tuneB;
   for (const SceneHost& h : s->sc) sch.K = std::max(sch.K, h.iterations);
   sch.pbf.assign(sch.K, 0);
   for (const SceneHost& h : s->sc) {
@@ -419,9 +424,9 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
   const int aflags = (sch.reduce ? kTrackResid : 0) | (sch.mode != 0 ? kWarm : 0);
   int in = 0;
   for (int k = 0; k < sch.K; ++k) {
-    launch_solveA(b, k, b.velS[in], aflags, st);
+    launch_solveA(b, k, b.velS[in], aflags, sch.varA, st);
     R.mark(st, "solveA");
-    launch_solveB(b, k, b.velS[in], b.velS[in ^ 1], sch.pbf[k] != 0, sch.reduce ? kTrackResid : 0, st);
+    launch_solveB(b, k, b.velS[in], b.velS[in ^ 1], sch.pbf[k] != 0, sch.reduce ? kTrackResid : 0, sch.varB, st);
     R.mark(st, "solveB");
     if (sch.reduce) {
       launch_resid_reduce(b, k, (aflags & kWarm) != 0, st);
@@ -437,9 +442,9 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
     }
   }
   if (sch.track) {  // residual of the state the iterations leave behind
-    launch_solveA(b, sch.K, b.velS[in], kTrackResid | kMeasureOnly, st);
+    launch_solveA(b, sch.K, b.velS[in], kTrackResid | kMeasureOnly, sch.varA, st);
     R.mark(st, "solveA(measure)");
-    launch_solveB(b, sch.K, b.velS[in], nullptr, false, kTrackResid | kMeasureOnly, st);
+    launch_solveB(b, sch.K, b.velS[in], nullptr, false, kTrackResid | kMeasureOnly, sch.varB, st);
     R.mark(st, "solveB(measure)");
     launch_resid_reduce(b, -1, false, st);
     R.mark(st, "residual");
@@ -969,6 +974,108 @@ int xpbi_profile_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water, f
     labels[m] = 0;
   }
   return checkDeviceErr(sim);
+}
+
+int xpbi_autotune(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t repeats, int32_t* chosen,
+                  float* ms, int32_t cap) {
+  XPBI_TRY(checkSim(sim));
+  for (const SceneHost& h : sim->sc)
+    if (!(h.params.dt > 0.f)) return fail(XPBI_ERR_INVALID, "write_params must be called before xpbi_autotune");
+  if (repeats < 1 || repeats > 1000) return fail(XPBI_ERR_INVALID, "repeats must be 1..1000");
+  XPBI_TRY(applySchedule(sim, iterations, has_water));
+  XPBI_TRY(upload(sim));
+  const Bufs& b = sim->b;
+  cudaStream_t st = sim->stream;
+  float t[kSolveAVariants + kSolveBVariants] = {0.f};
+  if (b.N > 0) {
+    // what read_state reports of the last substep and the timing runs
+    // overwrite (sort outputs, Bonet-Lok correction, multipliers): keep it
+    struct Saved {
+      void* dev;
+      size_t bytes;
+    };
+    const Saved keep[] = {{b.sortedIdx, 4 * (size_t)b.N},
+                          {b.cellStart, 4 * ((size_t)b.C + 1)},
+                          {b.L, 36 * (size_t)b.N},
+                          {b.lam, 4 * (size_t)b.N}};
+    size_t total = 0;
+    for (const Saved& k : keep) total += (k.bytes + 255) & ~(size_t)255;
+    uint8_t* save = nullptr;
+    if (cudaMalloc(&save, total) != cudaSuccess) return fail(XPBI_ERR_OOM, "xpbi_autotune scratch");
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    auto timed = [&](auto&& launch) {
+      launch();  // warm-up
+      cudaEventRecord(e0, st);
+      for (int r = 0; r < repeats; ++r) launch();
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      float x = 0.f;
+      cudaEventElapsedTime(&x, e0, e1);
+      return x / repeats;
+    };
+    {
+      size_t off = 0;
+      for (const Saved& k : keep) {
+        cudaMemcpyAsync(save + off, k.dev, k.bytes, cudaMemcpyDeviceToDevice, st);
+        off += (k.bytes + 255) & ~(size_t)255;
+      }
+    }
+    // the substep's preparation on the current state; it writes only the
+    // substep's working buffers, which the next substep rewrites
+    launch_count(b, st);
+    launch_scan(b, st);
+    launch_scatter(b, st);
+    launch_reorder(b, false, st);
+    launch_computeL(b, st);
+    cudaMemsetAsync(b.done, 0, sizeof(int) * b.S, st);  // no scene counts as converged here
+    // iteration 0 of each variant from lambda = 0, then solveB on its record
+    for (int v = 0; v < kSolveAVariants; ++v)
+      t[v] = timed([&] { launch_solveA(b, 0, b.velS[0], 0, v, st); });
+    int bestA = 0;
+    for (int v = 1; v < kSolveAVariants; ++v)
+      if (t[v] < t[bestA]) bestA = v;
+    if (t[0] <= 1.01f * t[bestA]) bestA = 0;  // keep the default on a near tie
+    launch_solveA(b, 0, b.velS[0], 0, bestA, st);
+    for (int v = 0; v < kSolveBVariants; ++v)
+      t[kSolveAVariants + v] = timed([&] { launch_solveB(b, 0, b.velS[0], b.velS[1], false, 0, v, st); });
+    int bestB = 0;
+    for (int v = 1; v < kSolveBVariants; ++v)
+      if (t[kSolveAVariants + v] < t[kSolveAVariants + bestB]) bestB = v;
+    if (t[kSolveAVariants] <= 1.01f * t[kSolveAVariants + bestB]) bestB = 0;
+    {
+      size_t off = 0;
+      for (const Saved& k : keep) {
+        cudaMemcpyAsync(k.dev, save + off, k.bytes, cudaMemcpyDeviceToDevice, st);
+        off += (k.bytes + 255) & ~(size_t)255;
+      }
+    }
+    const cudaError_t e = cudaStreamSynchronize(st);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(save);
+    if (e != cudaSuccess) return fail(XPBI_ERR_CUDA, std::string("xpbi_autotune: ") + cudaGetErrorString(e));
+    XPBI_CK(cudaGetLastError());
+    sim->tuneA = bestA;
+    sim->tuneB = bestB;
+  }
+  if (chosen) {
+    chosen[0] = sim->tuneA;
+    chosen[1] = sim->tuneB;
+  }
+  for (int k = 0; k < cap && k < kSolveAVariants + kSolveBVariants; ++k)
+    if (ms) ms[k] = t[k];
+  return checkDeviceErr(sim);
+}
+
+int xpbi_set_variants(xpbi_sim* sim, int32_t solve_a, int32_t solve_b) {
+  XPBI_TRY(checkSim(sim));
+  if (solve_a >= kSolveAVariants || solve_b >= kSolveBVariants)
+    return fail(XPBI_ERR_INVALID, "variant index out of range");
+  if (solve_a >= 0) sim->tuneA = solve_a;
+  if (solve_b >= 0) sim->tuneB = solve_b;
+  return XPBI_OK;
 }
 
 int xpbi_device_ptrs(xpbi_sim* sim, void** pos4, void** vel4, void** materials) {

@@ -46,22 +46,15 @@ constexpr int kThreads = 128;
 #else
 #define XPBI_LB_COMPUTEL XPBI_LB_DEFAULT
 #endif
-// solveA: 7 CTAs per SM (72 registers, a few spills outside the neighbour
-// loop) measured 15% faster than the allocator's own choice (88 registers,
-// 5 CTAs) on the 4M-particle dam-breach mix; 8 CTAs (64) spills in the loop
-#ifndef XPBI_MINB_SOLVEA
-#define XPBI_MINB_SOLVEA 7
-#endif
-// the tracked variant (residual stores) has its own override
-#ifndef XPBI_MINB_SOLVEA_TRACK
-#define XPBI_MINB_SOLVEA_TRACK 7
-#endif
-#define XPBI_LB_SOLVEA __launch_bounds__(kThreads, kTrack ? XPBI_MINB_SOLVEA_TRACK : XPBI_MINB_SOLVEA)
-#ifdef XPBI_MINB_SOLVEB
-#define XPBI_LB_SOLVEB __launch_bounds__(kThreads, XPBI_MINB_SOLVEB)
-#else
-#define XPBI_LB_SOLVEB XPBI_LB_DEFAULT
-#endif
+// solveA and solveB are compiled in several register-allocation variants
+// (the minimum resident CTAs per SM asked of the allocator; 0 = its own
+// choice), and xpbi_autotune picks one per handle by timing them on its
+// data. Entry 0 is the default: for solveA 7 CTAs per SM (72 registers, a
+// few spills outside the neighbour loop) measured 15% faster than the
+// allocator's own choice on the 4M-particle dam-breach mix; for solveB the
+// allocator's choice (80 registers) beat every cap.
+constexpr int kSolveAMinB[kSolveAVariants] = {7, 6, 5, 8};
+constexpr int kSolveBMinB[kSolveBVariants] = {0, 7, 5};
 #ifdef XPBI_MINB_PBF
 #define XPBI_LB_PBF __launch_bounds__(kThreads, XPBI_MINB_PBF)
 #else
@@ -394,8 +387,9 @@ __device__ __forceinline__ bool sceneDone(const Bufs& b, uint32_t i) {
 //   replaced by the plain start lambda0 = 0 (the plain solve stays the
 //   fallback). With lambda0 = 0 both updates are the reference's.
 // flags & kMeasureOnly: residual only (the pass after the last iteration).
-template <bool kTrack>
-__global__ void XPBI_LB_SOLVEA k_solveA(Bufs b, int k, const float4* __restrict__ velIn, int flags) {
+template <bool kTrack, int kMinB>
+__global__ void __launch_bounds__(kThreads, kMinB) k_solveA(Bufs b, int k, const float4* __restrict__ velIn,
+                                                            int flags) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
@@ -653,7 +647,8 @@ struct SBData {
 //   entering this iteration to rc (the contact residual; 0 for water).
 // flags & kMeasureOnly: the contact residual only, of every solid slot, no
 //   velocity update (the pass after the last iteration).
-__global__ void XPBI_LB_SOLVEB k_solveB(Bufs b, int k, const float4* __restrict__ velIn,
+template <int kMinB>
+__global__ void __launch_bounds__(kThreads, kMinB) k_solveB(Bufs b, int k, const float4* __restrict__ velIn,
                                                       float4* __restrict__ velOut, int writeXc, int flags) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
@@ -957,11 +952,20 @@ inline unsigned grid(uint32_t n) { return (unsigned)((n + kThreads - 1) / kThrea
 }  // namespace
 
 void launch_computeL(const Bufs& b, cudaStream_t st) { k_computeL<<<grid(b.N), kThreads, 0, st>>>(b); }
-void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, cudaStream_t st) {
+template <int V>
+void solveAVariant(const Bufs& b, int k, const float4* velIn, int flags, cudaStream_t st) {
   if (flags & kTrackResid)
-    k_solveA<true><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, flags);
+    k_solveA<true, kSolveAMinB[V]><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, flags);
   else
-    k_solveA<false><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, flags);
+    k_solveA<false, kSolveAMinB[V]><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, flags);
+}
+void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, int variant, cudaStream_t st) {
+  switch (variant) {
+    case 1: solveAVariant<1>(b, k, velIn, flags, st); break;
+    case 2: solveAVariant<2>(b, k, velIn, flags, st); break;
+    case 3: solveAVariant<3>(b, k, velIn, flags, st); break;
+    default: solveAVariant<0>(b, k, velIn, flags, st); break;
+  }
 }
 void launch_features(const Bufs& b, const float4* velIn, cudaStream_t st) {
   k_features<<<grid(b.N), kThreads, 0, st>>>(b, velIn);
@@ -973,9 +977,14 @@ void launch_resid_reduce(const Bufs& b, int k, bool warm, cudaStream_t st) {
   k_resid_final<<<(b.S + 3) / 4, 128, 0, st>>>(b, k, warm ? 1 : 0);
 }
 void launch_keep_lambda(const Bufs& b, cudaStream_t st) { k_keep_lambda<<<grid(b.N), kThreads, 0, st>>>(b); }
-void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, int flags,
+void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, int flags, int variant,
                    cudaStream_t st) {
-  k_solveB<<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, writeXc ? 1 : 0, flags);
+  const int wx = writeXc ? 1 : 0;
+  switch (variant) {
+    case 1: k_solveB<kSolveBMinB[1]><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, wx, flags); break;
+    case 2: k_solveB<kSolveBMinB[2]><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, wx, flags); break;
+    default: k_solveB<kSolveBMinB[0]><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, wx, flags); break;
+  }
 }
 void launch_pbfA(const Bufs& b, int k, const float4* velIn, cudaStream_t st) {
   (void)velIn;  // predicted positions were stored by the preceding solveB

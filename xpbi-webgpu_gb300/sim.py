@@ -261,6 +261,20 @@ class Simulation:
         del it
         return out, used.value
 
+    SOLVEA_VARIANTS, SOLVEB_VARIANTS = 4, 3
+
+    def autotune(self, iterations: int = -1, has_water: bool = True, repeats: int = 5) -> dict:
+        """Time every solveA / solveB variant on this handle's data and keep
+        the fastest (xpbi_autotune); returns the choice and the timings."""
+        chosen = (C.c_int32 * 2)()
+        ms = np.zeros(self.SOLVEA_VARIANTS + self.SOLVEB_VARIANTS, np.float32)
+        check(lib().xpbi_autotune(self._h, iterations, 1 if has_water else 0, repeats, chosen, _fptr(ms), len(ms)))
+        return {"solveA": int(chosen[0]), "solveB": int(chosen[1]),
+                "solveA_ms": ms[:self.SOLVEA_VARIANTS].tolist(), "solveB_ms": ms[self.SOLVEA_VARIANTS:].tolist()}
+
+    def set_variants(self, solve_a: int = -1, solve_b: int = -1):
+        check(lib().xpbi_set_variants(self._h, solve_a, solve_b))
+
     def read_contact_residuals(self, scene: int = 0):
         """Contact residual norms in the slots of read_residuals."""
         out = np.full(256, np.nan)
