@@ -165,3 +165,73 @@ def test_profile_substep_labels(xp, built_lib):
     assert len(lines) == n - 1  # the crowded-cell pass is timed with the reorder
     assert lines[0].startswith("count:") and lines[-1].startswith("updateF+integrate:")
     assert sum(1 for l in lines if l.startswith("pbfB:")) == 3
+
+
+def _clump(xp, sc, oracle, warm, count, material_kind):
+    """Move `count` particles of one material into a ball of radius 0.3 h:
+    their neighbour lists overflow the 64-entry record (every list-driven
+    pass falls back to the stencil walk) and their cell's bucket passes the
+    64 members of the rank rule (the crowded-bucket sort)."""
+    p = xp.params_for(sc)
+    it = sc["iterations"]
+    rng = np.random.default_rng(11)
+    with xp.Simulation(sc) as sim:
+        sim.write_params(p)
+        if warm:
+            sim.step(warm, it, sc["hasWater"])
+        st = sim.read_state()
+        kinds = np.array([m["kind"] for m in sc["materials"]])
+        idx = np.flatnonzero(kinds[np.abs(st["pos"][:, 3]).astype(int)] == material_kind)[:count]
+        centre = st["pos"][idx, :3].mean(axis=0)
+        u = rng.normal(size=(len(idx), 3))
+        u *= (0.3 * sc["h"] * rng.uniform(0, 1, len(idx)) ** (1 / 3) / np.linalg.norm(u, axis=1))[:, None]
+        pos = st["pos"].copy()
+        pos[idx, :3] = (centre + u).astype(np.float32)
+        sim.write_state(0, pos=pos)
+        s0 = sim.read_state()
+        pw, mw = sim.uniforms()
+        pi = p.get("pbfIterations")
+        pi = -1 if pi is None else int(pi)
+        ref = oracle.substep(pw, mw, s0, it, sc["hasWater"], pi)
+        ref64 = oracle.substep(pw, mw, s0, it, sc["hasWater"], pi, f64=True)
+        sim.encode_substep(it, sc["hasWater"])
+        s1 = sim.read_state()
+    assert len(idx) == count
+    return s0, s1, ref, ref64, p
+
+
+def test_crowded_clump_sand(xp, oracle, built_lib):
+    sc = xp.scenes.config_sand_column()
+    s0, s1, ref, ref64, p = _clump(xp, sc, oracle, 0, 150, 1)
+    compare(s1, ref, ref64, perturbed=perturbed_runs(oracle, sc, s0, xp=xp))
+
+
+def test_crowded_clump_water(xp, oracle, built_lib):
+    sc = xp.scenes.config_dam_breach(scale=0.05)
+    s0, s1, ref, ref64, p = _clump(xp, sc, oracle, 5, 150, 6)
+    compare(s1, ref, ref64, has_pbf=True, perturbed=perturbed_runs(oracle, sc, s0, xp=xp))
+
+
+def test_batch_with_an_empty_scene(xp, oracle, built_lib):
+    """A batch whose first scene has no particles: the others step as alone."""
+    empty = dict(xp.scenes.plasticine())
+    empty["positions"] = np.zeros((0, 3), np.float32)
+    empty["matIds"] = np.zeros(0, np.uint32)
+    for k in ("states", "velocities", "colorSeeds"):
+        empty.pop(k, None)
+    scenes = [empty, xp.scenes.snowball_smash(), xp.scenes.goo()]
+    with xp.Simulation(scenes) as sim:
+        for k, sc in enumerate(scenes):
+            sim.write_params(xp.params_for(sc), scene=k)
+            sim.set_schedule(k, sc["iterations"], sc["hasWater"])
+        sim.step(3, -1, False)
+        states = [sim.read_state(k) for k in range(1, 3)]
+        uni = [sim.uniforms(k) for k in range(1, 3)]
+        sim.encode_substep(-1, False)
+        after = [sim.read_state(k) for k in range(1, 3)]
+        assert len(sim.read_state(0)["pos"]) == 0
+    for k, sc in enumerate(scenes[1:]):
+        pw, mw = uni[k]
+        ref = oracle.substep(pw, mw, states[k], sc["iterations"], sc["hasWater"], -1)
+        ref64 = oracle.substep(pw, mw, states[k], sc["iterations"], sc["hasWater"], -1, f64=True)
+        compare(after[k], ref, ref64, has_pbf=sc["hasWater"])
