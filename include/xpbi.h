@@ -184,6 +184,33 @@ int xpbi_device_ptrs(xpbi_sim* sim, void** pos4, void** vel4, void** materials);
 /* Number of kernel launches one substep issues with this schedule. */
 int xpbi_launches_per_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t* out);
 
+/* ---- headless renderer (web/js/shaders/render.js, main.js:232-272) ----
+ * The reference draws each frame through WebGPU: the ground plane with its
+ * grid, the domain box, and every particle as a depth-correct sphere
+ * impostor (material colour with a per-particle shade, diffuse +
+ * hemisphere + specular lighting, water rims and speed whitening). This
+ * rasterises the same frame with CUDA kernels into a device RGBA8 image,
+ * with no graphics API. The camera is the reference's look-at camera
+ * (main.js:24-32 gives eye from its orbit angles; fov_y pi/4, near 0.02,
+ * far 50, light (0.5, 0.9, 0.35)); particle_radius <= 0 uses 0.62 h. */
+typedef struct xpbi_camera {
+  float eye[3];
+  float target[3];
+  float fov_y;             /* radians */
+  float near_z, far_z;
+  float light_dir[3];      /* world; normalised here */
+  float particle_radius;   /* world units; <= 0: 0.62 h of the scene */
+  int32_t draw_ground;     /* ground quad with grid lines at domain_min.y */
+  int32_t draw_box;        /* the 12 edges of the scene's domain */
+} xpbi_camera;
+
+/* Render scene `scene` at width x height (row 0 at the top, RGBA8). rgba_out
+ * (host, 4 * width * height bytes) and device_rgba (receives the device
+ * image, valid until the next xpbi_render or xpbi_destroy) may be NULL.
+ * Enqueued on the handle's stream; synchronous when rgba_out is given. */
+int xpbi_render(xpbi_sim* sim, uint32_t scene, const xpbi_camera* cam, uint32_t width, uint32_t height,
+                uint8_t* rgba_out, void** device_rgba);
+
 /* ---- autotuner (no counterpart in the reference) ----
  * solveA and solveB are built in several register-allocation variants
  * (resident blocks per SM traded against registers). xpbi_autotune runs the

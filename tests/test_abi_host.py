@@ -97,3 +97,20 @@ def test_empty_scene_packs(xp, built_lib):
     sc["colorSeeds"] = np.zeros(0, np.float32)
     pw, _ = xp.pack_uniforms(sc, xp.params_for(sc))
     assert int(pw[28]) == 0
+
+
+def test_render_camera_follows_main_js(xp):
+    import math
+    cam = xp.render.camera()  # scenes.js:90 orbit
+    t, p, d, tgt = 0.5, 0.32, 2.1, [0.5, 0.28, 0.5]
+    want = [tgt[0] + d * math.cos(p) * math.sin(t), tgt[1] + d * math.sin(p), tgt[2] + d * math.cos(p) * math.cos(t)]
+    assert np.allclose(list(cam.eye), want, rtol=1e-6)
+    assert cam.fov_y == pytest.approx(math.pi / 4) and cam.near_z == pytest.approx(0.02) and cam.far_z == 50
+
+
+def test_ppm_writer(xp, tmp_path):
+    img = np.zeros((2, 3, 4), np.uint8)
+    img[0, 1, :3] = (10, 20, 30)
+    xp.render.write_ppm(str(tmp_path / "a.ppm"), img)
+    data = (tmp_path / "a.ppm").read_bytes()
+    assert data.startswith(b"P6\n3 2\n255\n") and data[len(b"P6\n3 2\n255\n") + 3:][:3] == bytes((10, 20, 30))

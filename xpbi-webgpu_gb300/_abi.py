@@ -30,6 +30,7 @@ EXPORTS = (
     "xpbi_mlp_param_count", "xpbi_mlp_forward", "xpbi_mlp_grad", "xpbi_mlp_train",
     "xpbi_set_solver", "xpbi_set_network", "xpbi_read_residuals", "xpbi_read_training",
     "xpbi_sort_cells_noalloc", "xpbi_read_contact_residuals", "xpbi_autotune", "xpbi_set_variants",
+    "xpbi_render",
 )
 
 
@@ -51,6 +52,12 @@ class SceneDesc(C.Structure):
                 ("color_seeds", C.POINTER(C.c_float)), ("h", C.c_double),
                 ("domain_min", C.c_double * 3), ("domain_max", C.c_double * 3),
                 ("n_materials", C.c_uint32), ("materials", C.POINTER(Material))]
+
+
+class Camera(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("target", C.c_float * 3), ("fov_y", C.c_float), ("near_z", C.c_float),
+                ("far_z", C.c_float), ("light_dir", C.c_float * 3), ("particle_radius", C.c_float),
+                ("draw_ground", C.c_int32), ("draw_box", C.c_int32)]
 
 
 class Params(C.Structure):
@@ -102,6 +109,8 @@ _SIGS = {
     "xpbi_read_contact_residuals": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_double), C.c_int32]),
     "xpbi_autotune": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32), _F32P, C.c_int32]),
     "xpbi_set_variants": (C.c_int, [_P, C.c_int32, C.c_int32]),
+    "xpbi_render": (C.c_int, [_P, C.c_uint32, C.POINTER(Camera), C.c_uint32, C.c_uint32, C.POINTER(C.c_uint8),
+                              C.POINTER(_P)]),
     "xpbi_sort_cells_noalloc": (C.c_int, [_P, C.c_uint32, _F32P, C.c_float, C.POINTER(C.c_int32), _P, _P, _P]),
 }
 

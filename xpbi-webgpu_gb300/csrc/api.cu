@@ -16,6 +16,7 @@
 #include <string>
 #include <vector>
 
+#include "render.h"
 #include "xpbi.h"
 #include "xpbi_internal.h"
 
@@ -283,6 +284,10 @@ struct xpbi_sim {
   int* netErr = nullptr;
   // register-allocation variants of solveA / solveB (xpbi_autotune)
   int tuneA = 0, tuneB = 0;
+  // headless renderer targets (xpbi_render), sized on demand
+  unsigned long long* renderImg = nullptr;
+  uint32_t* renderRgba = nullptr;
+  size_t renderPixels = 0;
 };
 
 namespace {
@@ -308,6 +313,8 @@ void destroyAll(xpbi_sim* s) {
   if (s->gexec) cudaGraphExecDestroy(s->gexec);
   if (s->graph) cudaGraphDestroy(s->graph);
   for (void* p : s->allocs) cudaFree(p);
+  if (s->renderImg) cudaFree(s->renderImg);
+  if (s->renderRgba) cudaFree(s->renderRgba);
   if (s->own) cudaStreamDestroy(s->own);
   if (s->capture) cudaStreamDestroy(s->capture);
 }
@@ -1076,6 +1083,100 @@ int xpbi_set_variants(xpbi_sim* sim, int32_t solve_a, int32_t solve_b) {
   if (solve_a >= 0) sim->tuneA = solve_a;
   if (solve_b >= 0) sim->tuneB = solve_b;
   return XPBI_OK;
+}
+
+namespace {
+// main.js:33-62 in f64, stored as f32 like the reference's Float32Array
+void lookAt(const double eye[3], const double tgt[3], float out[16]) {
+  auto norm = [](double v[3]) {
+    const double l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    for (int k = 0; k < 3; ++k) v[k] /= l;
+  };
+  double z[3] = {eye[0] - tgt[0], eye[1] - tgt[1], eye[2] - tgt[2]};
+  norm(z);
+  const double up[3] = {0, 1, 0};
+  double x[3] = {up[1] * z[2] - up[2] * z[1], up[2] * z[0] - up[0] * z[2], up[0] * z[1] - up[1] * z[0]};
+  norm(x);
+  const double y[3] = {z[1] * x[2] - z[2] * x[1], z[2] * x[0] - z[0] * x[2], z[0] * x[1] - z[1] * x[0]};
+  auto dot = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+  const double m[16] = {x[0], y[0], z[0], 0, x[1], y[1], z[1], 0, x[2], y[2], z[2], 0,
+                        -dot(x, eye), -dot(y, eye), -dot(z, eye), 1};
+  for (int k = 0; k < 16; ++k) out[k] = (float)m[k];
+}
+void perspective(double fovY, double aspect, double nearZ, double farZ, float out[16]) {
+  const double f = 1.0 / std::tan(fovY / 2);
+  const double m[16] = {f / aspect, 0, 0, 0, 0, f, 0, 0, 0, 0, farZ / (nearZ - farZ), -1,
+                        0, 0, (nearZ * farZ) / (nearZ - farZ), 0};
+  for (int k = 0; k < 16; ++k) out[k] = (float)m[k];
+}
+void mul4(const float a[16], const float b[16], float out[16]) {  // a * b, column-major
+  for (int c = 0; c < 4; ++c)
+    for (int r = 0; r < 4; ++r) {
+      double s = 0;
+      for (int k = 0; k < 4; ++k) s += (double)a[k * 4 + r] * (double)b[c * 4 + k];
+      out[c * 4 + r] = (float)s;
+    }
+}
+}  // namespace
+
+int xpbi_render(xpbi_sim* sim, uint32_t scene, const xpbi_camera* cam, uint32_t width, uint32_t height,
+                uint8_t* rgba_out, void** device_rgba) {
+  XPBI_TRY(checkSim(sim));
+  if (!cam) return fail(XPBI_ERR_INVALID, "camera is NULL");
+  if (scene >= sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
+  if (width < 1 || height < 1 || width > 16384 || height > 16384)
+    return fail(XPBI_ERR_INVALID, "image size must be 1..16384 per side");
+  if (!(cam->fov_y > 0.f && cam->fov_y < 3.1f) || !(cam->near_z > 0.f && cam->far_z > cam->near_z))
+    return fail(XPBI_ERR_INVALID, "camera needs 0 < fov_y < pi and 0 < near_z < far_z");
+  XPBI_TRY(upload(sim));
+  const SceneHost& h = sim->sc[scene];
+  RenderParams P{};
+  const double eye[3] = {cam->eye[0], cam->eye[1], cam->eye[2]};
+  const double tgt[3] = {cam->target[0], cam->target[1], cam->target[2]};
+  if (eye[0] == tgt[0] && eye[1] == tgt[1] && eye[2] == tgt[2]) return fail(XPBI_ERR_INVALID, "eye equals target");
+  lookAt(eye, tgt, P.view);
+  perspective(cam->fov_y, (double)width / height, cam->near_z, cam->far_z, P.proj);
+  mul4(P.proj, P.view, P.viewProj);
+  for (int k = 0; k < 3; ++k) {
+    P.eye[k] = cam->eye[k];
+    P.boxMin[k] = (float)h.dmin[k];
+    P.boxMax[k] = (float)h.dmax[k];
+  }
+  const double l = std::sqrt((double)cam->light_dir[0] * cam->light_dir[0] +
+                             (double)cam->light_dir[1] * cam->light_dir[1] +
+                             (double)cam->light_dir[2] * cam->light_dir[2]);
+  if (!(l > 0)) return fail(XPBI_ERR_INVALID, "light_dir must be nonzero");
+  for (int k = 0; k < 3; ++k) P.lightDir[k] = (float)(cam->light_dir[k] / l);
+  P.particleRadius = cam->particle_radius > 0.f ? cam->particle_radius : (float)(h.h * 0.62);
+  P.groundY = (float)h.dmin[1];
+  P.nearZ = cam->near_z;
+  P.width = (int)width;
+  P.height = (int)height;
+  P.drawGround = cam->draw_ground ? 1 : 0;
+  P.drawBox = cam->draw_box ? 1 : 0;
+  P.maxPixelsPerParticle = 1 << 16;
+  const size_t pixels = (size_t)width * height;
+  if (pixels > sim->renderPixels) {
+    if (sim->renderImg) cudaFree(sim->renderImg);
+    if (sim->renderRgba) cudaFree(sim->renderRgba);
+    sim->renderImg = nullptr;
+    sim->renderRgba = nullptr;
+    sim->renderPixels = 0;
+    if (cudaMalloc(&sim->renderImg, 8 * pixels) != cudaSuccess ||
+        cudaMalloc(&sim->renderRgba, 4 * pixels) != cudaSuccess)
+      return fail(XPBI_ERR_OOM, "render target allocation failed");
+    sim->renderPixels = pixels;
+  }
+  const Bufs& b = sim->b;
+  render_frame(P, b.pos + h.pBase, b.vel + h.pBase, sim->matWords + (size_t)scene * kMaxMats * XPBI_MATERIAL_WORDS,
+               h.n, sim->renderImg, sim->renderRgba, sim->stream);
+  XPBI_CK(cudaGetLastError());
+  if (rgba_out) {
+    XPBI_CK(cudaMemcpyAsync(rgba_out, sim->renderRgba, 4 * pixels, cudaMemcpyDeviceToHost, sim->stream));
+    XPBI_CK(cudaStreamSynchronize(sim->stream));
+  }
+  if (device_rgba) *device_rgba = sim->renderRgba;
+  return checkDeviceErr(sim);
 }
 
 int xpbi_device_ptrs(xpbi_sim* sim, void** pos4, void** vel4, void** materials) {

@@ -91,7 +91,8 @@ def base(h):
     """Solver defaults (scenes.js:82-92)."""
     return dict(h=h, domainMin=[0.0, 0.0, 0.0], domainMax=[1.0, 1.0, 1.0], gravity=[0.0, -9.8, 0.0],
                 substeps=8, iterations=3, timeScale=0.42, omega=0.5, contactOmega=0.4, xsphC=0.01,
-                pbfEps=100.0, sCorrK=0.0001, kDamp=0.4)
+                pbfEps=100.0, sCorrK=0.0001, kDamp=0.4,
+                camera=dict(theta=0.5, phi=0.32, dist=2.1, target=[0.5, 0.28, 0.5]))
 
 
 def _finish(s, rng, pos, mid, st, materials, has_water, velocities=None):
