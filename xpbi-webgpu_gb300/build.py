@@ -47,7 +47,7 @@ def build(verbose: bool = False, ptxas_v: bool = False, force: bool = False, out
           extra: list[str] | None = None, build_dir: str | None = None) -> str:
     """Compile every .cu for sm_103a and link libxpbi.so; returns its path.
 
-    out / build_dir / extra (nvcc flags such as -DXPBI_MINB_SOLVEB=8) build
+    out / build_dir / extra (nvcc flags such as -DXPBI_MINB_PBF=8) build
     a variant of the library elsewhere without touching the default one."""
     lib = out or LIB
     bdir = build_dir or BUILD
