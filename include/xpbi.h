@@ -231,6 +231,14 @@ int xpbi_autotune(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t 
 /* Select variants directly (-1 keeps the current one); 0 is the default. */
 int xpbi_set_variants(xpbi_sim* sim, int32_t solve_a, int32_t solve_b);
 
+/* Lanes per particle in solveA / solveB: 1, 4, or 0 (the default) for four
+ * when the handle holds at most 65,536 particles. Small scenes leave most of
+ * the GPU idle with one thread per particle; four lanes split each
+ * particle's neighbour sweep and add their partial sums, which changes the
+ * summation order (results agree with one lane to rounding, not bit for
+ * bit). The register variants above apply to the one-lane kernels. */
+int xpbi_set_lanes(xpbi_sim* sim, int32_t lanes);
+
 /* ---- solver modes (no counterpart in the reference) ----
  * mode 0: the reference solve (every XPBI iteration starts from lambda = 0).
  * mode 1: iteration 0 starts from the particle's previous-substep multiplier

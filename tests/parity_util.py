@@ -48,8 +48,10 @@ def rel(a, b) -> float:
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
 
 
-def run_pair(xp, O, scene, warm: int = 0, iterations=None, has_water=None, params=None, threads: int = 0):
-    """(state before, GPU state after, f32 oracle after, f64 oracle after)."""
+def run_pair(xp, O, scene, warm: int = 0, iterations=None, has_water=None, params=None, threads: int = 0,
+             lanes: int = 0):
+    """(state before, GPU state after, f32 oracle after, f64 oracle after);
+    lanes: lanes per particle of solveA / solveB (0: the library's choice)."""
     p = xp.params_for(scene) if params is None else params
     it = scene["iterations"] if iterations is None else iterations
     hw = scene["hasWater"] if has_water is None else has_water
@@ -57,6 +59,7 @@ def run_pair(xp, O, scene, warm: int = 0, iterations=None, has_water=None, param
     pi = -1 if pi is None else int(pi)
     with xp.Simulation(scene) as sim:
         sim.write_params(p)
+        sim.set_lanes(lanes)
         if warm:
             sim.step(warm, it, hw)
         s0 = sim.read_state()

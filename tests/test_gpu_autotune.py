@@ -14,6 +14,7 @@ FIELDS = ("pos", "vel", "F", "L", "aux", "sortedIdx", "cellTab")
 def _run(xp, sc, variants, substeps=4):
     with xp.Simulation(sc) as sim:
         sim.write_params(xp.params_for(sc))
+        sim.set_lanes(1)  # the register variants are the one-lane kernels
         sim.step(3, sc["iterations"], sc["hasWater"])
         if variants is not None:
             sim.set_variants(*variants)
@@ -36,6 +37,7 @@ def test_autotune_keeps_the_state_and_picks_a_variant(xp, built_lib):
     sc = xp.scenes.config_dam_breach(scale=0.05)
     with xp.Simulation(sc) as sim:
         sim.write_params(xp.params_for(sc))
+        sim.set_lanes(1)
         sim.step(5, sc["iterations"], True)
         before = sim.read_state()
         res = sim.autotune(sc["iterations"], True, repeats=3)

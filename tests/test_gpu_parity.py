@@ -167,7 +167,7 @@ def test_profile_substep_labels(xp, built_lib):
     assert sum(1 for l in lines if l.startswith("pbfB:")) == 3
 
 
-def _clump(xp, sc, oracle, warm, count, material_kind):
+def _clump(xp, sc, oracle, warm, count, material_kind, lanes=0):
     """Move `count` particles of one material into a ball of radius 0.3 h:
     their neighbour lists overflow the 64-entry record (every list-driven
     pass falls back to the stencil walk) and their cell's bucket passes the
@@ -177,6 +177,7 @@ def _clump(xp, sc, oracle, warm, count, material_kind):
     rng = np.random.default_rng(11)
     with xp.Simulation(sc) as sim:
         sim.write_params(p)
+        sim.set_lanes(lanes)
         if warm:
             sim.step(warm, it, sc["hasWater"])
         st = sim.read_state()
@@ -200,9 +201,10 @@ def _clump(xp, sc, oracle, warm, count, material_kind):
     return s0, s1, ref, ref64, p
 
 
-def test_crowded_clump_sand(xp, oracle, built_lib):
+@pytest.mark.parametrize("lanes", [1, 4])
+def test_crowded_clump_sand(xp, oracle, built_lib, lanes):
     sc = xp.scenes.config_sand_column()
-    s0, s1, ref, ref64, p = _clump(xp, sc, oracle, 0, 150, 1)
+    s0, s1, ref, ref64, p = _clump(xp, sc, oracle, 0, 150, 1, lanes)
     compare(s1, ref, ref64, perturbed=perturbed_runs(oracle, sc, s0, xp=xp))
 
 
@@ -235,3 +237,24 @@ def test_batch_with_an_empty_scene(xp, oracle, built_lib):
         ref = oracle.substep(pw, mw, states[k], sc["iterations"], sc["hasWater"], -1)
         ref64 = oracle.substep(pw, mw, states[k], sc["iterations"], sc["hasWater"], -1, f64=True)
         compare(after[k], ref, ref64, has_pbf=sc["hasWater"])
+
+
+@pytest.mark.parametrize("case", ["sand_flowing", "dam_breach", "snowball"])
+def test_one_lane_per_particle(xp, oracle, built_lib, case):
+    """The same substeps with one lane per particle in solveA / solveB (the
+    path large handles take; small ones default to four lanes)."""
+    if case == "sand_flowing":
+        sc, warm = xp.scenes.config_sand_column(), 300
+    elif case == "dam_breach":
+        sc, warm = xp.scenes.config_dam_breach(scale=0.05), 10
+    else:
+        sc, warm = xp.scenes.config_nacc_snowball(), 125
+    s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=warm, lanes=1)
+    compare(s1, ref, ref64, has_pbf=sc["hasWater"], perturbed=perturbed_runs(oracle, sc, s0, xp=xp))
+
+
+def test_four_lanes_on_a_large_handle(xp, oracle, built_lib):
+    """Four lanes forced on a handle above the automatic threshold."""
+    sc = xp.scenes.config_dam_breach(scale=0.3)
+    s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=5, lanes=4)
+    compare(s1, ref, ref64, has_pbf=True, perturbed=perturbed_runs(oracle, sc, s0, xp=xp))

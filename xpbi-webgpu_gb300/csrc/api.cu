@@ -284,6 +284,7 @@ struct xpbi_sim {
   int* netErr = nullptr;
   // register-allocation variants of solveA / solveB (xpbi_autotune)
   int tuneA = 0, tuneB = 0;
+  int lanesMode = 0;  // lanes per slot in solveA / solveB: 0 by size, 1 or 4
   // headless renderer targets (xpbi_render), sized on demand
   unsigned long long* renderImg = nullptr;
   uint32_t* renderRgba = nullptr;
@@ -351,11 +352,12 @@ struct Schedule {
   bool features = false; // network features at iteration 0
   bool keepLam = false;  // carry the final multipliers into the next substep
   int varA = 0, varB = 0; // solveA / solveB variants
+  int lanes = 1;          // lanes per slot in solveA / solveB
   std::string key() const {
     std::string k = std::to_string(K) + ":";
     for (char c : pbf) k += c ? '1' : '0';
     k += ":" + std::to_string(mode) + (track ? "t" : "") + (reduce ? "r" : "") + (features ? "f" : "") +
-         (keepLam ? "l" : "") + ":v" + std::to_string(varA) + std::to_string(varB);
+         (keepLam ? "l" : "") + ":v" + std::to_string(varA) + std::to_string(varB) + ":g" + std::to_string(lanes);
     return k;
   }
 };
@@ -369,6 +371,7 @@ Schedule schedule(const xpbi_sim* s) {
   sch.keepLam = s->mode != 0 || sch.features;
   sch.varA = s->tuneA;
   sch.varB = s->tuneB;
+  sch.lanes = s->lanesMode ? s->lanesMode : (s->b.N <= kSmallScene ? 4 : 1);
   for (const SceneHost& h : s->sc) sch.K = std::max(sch.K, h.iterations);
   sch.pbf.assign(sch.K, 0);
   for (const SceneHost& h : s->sc) {
@@ -431,9 +434,10 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
   const int aflags = (sch.reduce ? kTrackResid : 0) | (sch.mode != 0 ? kWarm : 0);
   int in = 0;
   for (int k = 0; k < sch.K; ++k) {
-    launch_solveA(b, k, b.velS[in], aflags, sch.varA, st);
+    launch_solveA(b, k, b.velS[in], aflags, sch.varA, sch.lanes, st);
     R.mark(st, "solveA");
-    launch_solveB(b, k, b.velS[in], b.velS[in ^ 1], sch.pbf[k] != 0, sch.reduce ? kTrackResid : 0, sch.varB, st);
+    launch_solveB(b, k, b.velS[in], b.velS[in ^ 1], sch.pbf[k] != 0, sch.reduce ? kTrackResid : 0, sch.varB,
+                  sch.lanes, st);
     R.mark(st, "solveB");
     if (sch.reduce) {
       launch_resid_reduce(b, k, (aflags & kWarm) != 0, st);
@@ -449,9 +453,9 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
     }
   }
   if (sch.track) {  // residual of the state the iterations leave behind
-    launch_solveA(b, sch.K, b.velS[in], kTrackResid | kMeasureOnly, sch.varA, st);
+    launch_solveA(b, sch.K, b.velS[in], kTrackResid | kMeasureOnly, sch.varA, sch.lanes, st);
     R.mark(st, "solveA(measure)");
-    launch_solveB(b, sch.K, b.velS[in], nullptr, false, kTrackResid | kMeasureOnly, sch.varB, st);
+    launch_solveB(b, sch.K, b.velS[in], nullptr, false, kTrackResid | kMeasureOnly, sch.varB, sch.lanes, st);
     R.mark(st, "solveB(measure)");
     launch_resid_reduce(b, -1, false, st);
     R.mark(st, "residual");
@@ -1039,14 +1043,14 @@ int xpbi_autotune(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t 
     cudaMemsetAsync(b.done, 0, sizeof(int) * b.S, st);  // no scene counts as converged here
     // iteration 0 of each variant from lambda = 0, then solveB on its record
     for (int v = 0; v < kSolveAVariants; ++v)
-      t[v] = timed([&] { launch_solveA(b, 0, b.velS[0], 0, v, st); });
+      t[v] = timed([&] { launch_solveA(b, 0, b.velS[0], 0, v, 1, st); });
     int bestA = 0;
     for (int v = 1; v < kSolveAVariants; ++v)
       if (t[v] < t[bestA]) bestA = v;
     if (t[0] <= 1.01f * t[bestA]) bestA = 0;  // keep the default on a near tie
-    launch_solveA(b, 0, b.velS[0], 0, bestA, st);
+    launch_solveA(b, 0, b.velS[0], 0, bestA, 1, st);
     for (int v = 0; v < kSolveBVariants; ++v)
-      t[kSolveAVariants + v] = timed([&] { launch_solveB(b, 0, b.velS[0], b.velS[1], false, 0, v, st); });
+      t[kSolveAVariants + v] = timed([&] { launch_solveB(b, 0, b.velS[0], b.velS[1], false, 0, v, 1, st); });
     int bestB = 0;
     for (int v = 1; v < kSolveBVariants; ++v)
       if (t[kSolveAVariants + v] < t[kSolveAVariants + bestB]) bestB = v;
@@ -1074,6 +1078,14 @@ int xpbi_autotune(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t 
   for (int k = 0; k < cap && k < kSolveAVariants + kSolveBVariants; ++k)
     if (ms) ms[k] = t[k];
   return checkDeviceErr(sim);
+}
+
+int xpbi_set_lanes(xpbi_sim* sim, int32_t lanes) {
+  XPBI_TRY(checkSim(sim));
+  if (lanes != 0 && lanes != 1 && lanes != 4) return fail(XPBI_ERR_INVALID, "lanes must be 0 (by size), 1 or 4");
+  if (lanes == 4 && sim->b.N > (1u << 28)) return fail(XPBI_ERR_INVALID, "four lanes per slot need N <= 2^28");
+  sim->lanesMode = lanes;
+  return XPBI_OK;
 }
 
 int xpbi_set_variants(xpbi_sim* sim, int32_t solve_a, int32_t solve_b) {

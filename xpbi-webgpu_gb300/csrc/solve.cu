@@ -176,6 +176,57 @@ __device__ __forceinline__ void forNbrs(const Bufs& b, const Ctx& cx, uint32_t i
   }
 }
 
+// Several lanes per slot (small scenes): the G lanes of slot i are
+// consecutive in the warp; lane `lane` visits the list entries k with
+// k % G == lane (each group of four entries is one load, shared by the four
+// lanes), or on the overflow walk every G-th candidate of each row. Each
+// lane accumulates a partial sum; laneSum adds them over the group.
+template <int G, class Gather, class Body>
+__device__ __forceinline__ void forNbrsLanes(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi, uint32_t lane,
+                                             Gather&& gather, Body&& body) {
+  static_assert(G == 1 || G == 4, "one or four lanes per slot");
+  if constexpr (G == 1) {
+    (void)lane;
+    forNbrs(b, cx, i, xi, gather, body);
+  } else {
+    const uint32_t cnt = b.nbrCount[i];
+    if (cnt != kNbrOverflow) {
+      const uint4* __restrict__ L = reinterpret_cast<const uint4*>(listOf(b.nbr, i));
+      const uint32_t groups = (cnt + 3u) >> 2;
+#pragma unroll 1
+      for (uint32_t q = 0; q < groups; ++q) {
+        const uint32_t e = lane4(__ldg(L + q), lane);
+        if (4u * q + lane < cnt) body(e & ~kWaterBit, (e & kWaterBit) != 0u, gather(e & ~kWaterBit));
+      }
+    } else {
+      const SceneDev& S = *cx.scene;
+      forRows(S, b.cellStart, xi, [&](uint32_t beg, uint32_t end) {
+#pragma unroll 1
+        for (uint32_t j = beg + lane; j < end; j += G) {
+          if (j == i) continue;
+          const float4 pj = ldg(b.posS + j);
+          const V3 d = xi - xyz(pj);
+          if (dot(d, d) < S.support2) body(j, waterW(pj.w), gather(j));
+        }
+      });
+    }
+  }
+}
+
+template <int G>
+__device__ __forceinline__ float laneSum(float v) {
+  if constexpr (G > 1) {
+    const unsigned group = 0xFu << (threadIdx.x & 28u);  // warp lanes 4p .. 4p+3
+    v += __shfl_xor_sync(group, v, 1);
+    v += __shfl_xor_sync(group, v, 2);
+  }
+  return v;
+}
+template <int G>
+__device__ __forceinline__ V3 laneSum(V3 v) {
+  return v3(laneSum<G>(v.x), laneSum<G>(v.y), laneSum<G>(v.z));
+}
+
 // Records, in stencil order, the candidates j != i of the rows around `x`
 // whose test(j) holds: list entry j | water bit from flag(j).
 template <class Test>
@@ -290,8 +341,10 @@ struct Constraint {
   float nNbr;     // solid neighbours in the sweep
 };
 
+template <int NL = 1>
 __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& cx, uint32_t i, float4 pi,
-                                                     const float4* __restrict__ velIn, const MatDev& m, float st) {
+                                                     const float4* __restrict__ velIn, const MatDev& m, float st,
+                                                     uint32_t lane = 0) {
   const SceneDev& S = *cx.scene;
   const float4* __restrict__ posS = b.posS;
   const V3 xi = xyz(pi);
@@ -304,7 +357,7 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
   M3 A = mzero();
   V3 sg = splat(0.f);
   float p00 = 0.f, p11 = 0.f, p22 = 0.f, p01 = 0.f, p02 = 0.f, p12 = 0.f, cnt = 0.f;
-  forNbrs(b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
+  forNbrsLanes<NL>(b, cx, i, xi, lane, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
           [&](uint32_t, bool water, const PV& d) {
             if (water) return;
             const V3 g = gradWFast(S, xi - xyz(d.p));
@@ -322,6 +375,19 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
             p12 += cg.y * g.z;
             cnt += 1.f;
           });
+  if constexpr (NL > 1) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) A.c[c] = laneSum<NL>(A.c[c]);
+    sg = laneSum<NL>(sg);
+    p00 = laneSum<NL>(p00);
+    p11 = laneSum<NL>(p11);
+    p22 = laneSum<NL>(p22);
+    p01 = laneSum<NL>(p01);
+    p02 = laneSum<NL>(p02);
+    p12 = laneSum<NL>(p12);
+    cnt = laneSum<NL>(cnt);
+    if (lane != 0) return Constraint{};  // lane 0 finishes the slot
+  }
   const M3 Li = loadM(b.L, b.N, i);
   const M3 LiT = transpose(Li);
   const M3 G = mul(A, LiT);
@@ -387,10 +453,13 @@ __device__ __forceinline__ bool sceneDone(const Bufs& b, uint32_t i) {
 //   replaced by the plain start lambda0 = 0 (the plain solve stays the
 //   fallback). With lambda0 = 0 both updates are the reference's.
 // flags & kMeasureOnly: residual only (the pass after the last iteration).
-template <bool kTrack, int kMinB>
+// G lanes per slot (G = 4 for small scenes): the lanes split the neighbour
+// sweep, lane 0 finishes the slot.
+template <bool kTrack, int kMinB, int G>
 __global__ void __launch_bounds__(kThreads, kMinB) k_solveA(Bufs b, int k, const float4* __restrict__ velIn,
                                                             int flags) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t / G, lane = t % G;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
@@ -400,7 +469,7 @@ __global__ void __launch_bounds__(kThreads, kMinB) k_solveA(Bufs b, int k, const
   const float4 pi = b.posS[i];
   const bool active = measure || (k < S.iterations && !sceneDone(b, i));
   if (!active || waterW(pi.w)) {  // water: its record is never read
-    if (track) {
+    if (track && lane == 0) {
       b.rr[i] = 0.f;
       if (k == 0) b.c0sq[i] = 0.f;
     }
@@ -409,7 +478,8 @@ __global__ void __launch_bounds__(kThreads, kMinB) k_solveA(Bufs b, int k, const
   const uint32_t mi = matOfW(pi.w);
   const float st = b.stateS[i];
   const MatDev m = hardenedMat(cx.mats[mi], st);
-  const Constraint c = evalConstraint(b, cx, i, pi, velIn, m, st);
+  const Constraint c = evalConstraint<G>(b, cx, i, pi, velIn, m, st, lane);
+  if (G > 1 && lane != 0) return;
   const float g = S.kDamp;
   const float stiff = (1.f + g) * c.denom + S.alphaT;  // d(residual) / d(applied multiplier)
   const float r0 = c.C + g * S.dt * c.cdot;            // residual at lambda = 0
@@ -647,10 +717,11 @@ struct SBData {
 //   entering this iteration to rc (the contact residual; 0 for water).
 // flags & kMeasureOnly: the contact residual only, of every solid slot, no
 //   velocity update (the pass after the last iteration).
-template <int kMinB>
+template <int kMinB, int G>
 __global__ void __launch_bounds__(kThreads, kMinB) k_solveB(Bufs b, int k, const float4* __restrict__ velIn,
                                                       float4* __restrict__ velOut, int writeXc, int flags) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t / G, lane = t % G;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
@@ -661,10 +732,12 @@ __global__ void __launch_bounds__(kThreads, kMinB) k_solveB(Bufs b, int k, const
   const bool track = (flags & kTrackResid) != 0;
   const bool measure = (flags & kMeasureOnly) != 0;
   if (!measure && (k >= S.iterations || sceneDone(b, i))) {
-    velOut[i] = vi4;
-    if (writeXc) {
-      const V3 xc = xyz(pi) + S.dt * xyz(vi4);
-      b.xc[i] = make_float4(xc.x, xc.y, xc.z, pi.w);
+    if (lane == 0) {
+      velOut[i] = vi4;
+      if (writeXc) {
+        const V3 xc = xyz(pi) + S.dt * xyz(vi4);
+        b.xc[i] = make_float4(xc.x, xc.y, xc.z, pi.w);
+      }
     }
     return;
   }
@@ -674,7 +747,7 @@ __global__ void __launch_bounds__(kThreads, kMinB) k_solveB(Bufs b, int k, const
   V3 dv = splat(0.f), corr = splat(0.f);
   if (!waterW(pi.w)) {
     const size_t N = b.N;
-    dv = xyz(b.SpSelf[i]);
+    if (G == 1) dv = xyz(b.SpSelf[i]);
     const float Vi = vi4.w;
     const V3 xci = xi + S.dt * xyz(vi4);
     const float minD = S.minD;
@@ -695,7 +768,19 @@ __global__ void __launch_bounds__(kThreads, kMinB) k_solveB(Bufs b, int k, const
       }
     };
     const uint32_t cnt = b.nbrCount[i];
-    if (cnt != kNbrOverflow) {
+    if (G > 1 && cnt != kNbrOverflow) {
+      // lane `lane` takes the entries k % G == lane, skipping water ones
+      const uint4* __restrict__ L = reinterpret_cast<const uint4*>(listOf(b.nbr, i));
+      const uint32_t groups = (cnt + 3u) >> 2;
+#pragma unroll 1
+      for (uint32_t q = 0; q < groups; ++q) {
+        const uint32_t e = lane4(__ldg(L + q), lane);
+        if (4u * q + lane < cnt && !(e & kWaterBit)) {
+          const float4* R = Sp + e;
+          body(false, SBData{ldg(R), ldg(R + N), ldg(R + 2 * N), ldg(R + 3 * N)});
+        }
+      }
+    } else if (G == 1 && cnt != kNbrOverflow) {
       // water neighbours are skipped before their record is loaded
       forList<true>(listOf(b.nbr, i), cnt,
                     [&](uint32_t e) {
@@ -715,7 +800,7 @@ __global__ void __launch_bounds__(kThreads, kMinB) k_solveB(Bufs b, int k, const
     } else {
       forRows(S, b.cellStart, xi, [&](uint32_t beg, uint32_t end) {
 #pragma unroll 1
-        for (uint32_t j = beg; j < end; ++j) {
+        for (uint32_t j = beg + lane; j < end; j += G) {
           if (j == i) continue;
           const float4 pj = ldg(posS + j);
           const V3 d = xi - xyz(pj);
@@ -726,7 +811,12 @@ __global__ void __launch_bounds__(kThreads, kMinB) k_solveB(Bufs b, int k, const
         }
       });
     }
+    if constexpr (G > 1) {
+      dv = laneSum<G>(dv) + xyz(b.SpSelf[i]);
+      corr = laneSum<G>(corr);
+    }
   }
+  if (G > 1 && lane != 0) return;
   if (track) b.rc[i] = dot(corr, corr);
   if (measure) return;
   V3 dvv = dv / (m.mass * S.dt);
@@ -955,11 +1045,19 @@ void launch_computeL(const Bufs& b, cudaStream_t st) { k_computeL<<<grid(b.N), k
 template <int V>
 void solveAVariant(const Bufs& b, int k, const float4* velIn, int flags, cudaStream_t st) {
   if (flags & kTrackResid)
-    k_solveA<true, kSolveAMinB[V]><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, flags);
+    k_solveA<true, kSolveAMinB[V], 1><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, flags);
   else
-    k_solveA<false, kSolveAMinB[V]><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, flags);
+    k_solveA<false, kSolveAMinB[V], 1><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, flags);
 }
-void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, int variant, cudaStream_t st) {
+void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, int variant, int lanes, cudaStream_t st) {
+  if (lanes == 4) {  // small scenes: four lanes per slot, the allocator's register choice
+    const uint32_t threads = 4u * b.N;
+    if (flags & kTrackResid)
+      k_solveA<true, 0, 4><<<grid(threads), kThreads, 0, st>>>(b, k, velIn, flags);
+    else
+      k_solveA<false, 0, 4><<<grid(threads), kThreads, 0, st>>>(b, k, velIn, flags);
+    return;
+  }
   switch (variant) {
     case 1: solveAVariant<1>(b, k, velIn, flags, st); break;
     case 2: solveAVariant<2>(b, k, velIn, flags, st); break;
@@ -978,12 +1076,16 @@ void launch_resid_reduce(const Bufs& b, int k, bool warm, cudaStream_t st) {
 }
 void launch_keep_lambda(const Bufs& b, cudaStream_t st) { k_keep_lambda<<<grid(b.N), kThreads, 0, st>>>(b); }
 void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, int flags, int variant,
-                   cudaStream_t st) {
+                   int lanes, cudaStream_t st) {
   const int wx = writeXc ? 1 : 0;
+  if (lanes == 4) {
+    k_solveB<0, 4><<<grid(4u * b.N), kThreads, 0, st>>>(b, k, velIn, velOut, wx, flags);
+    return;
+  }
   switch (variant) {
-    case 1: k_solveB<kSolveBMinB[1]><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, wx, flags); break;
-    case 2: k_solveB<kSolveBMinB[2]><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, wx, flags); break;
-    default: k_solveB<kSolveBMinB[0]><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, wx, flags); break;
+    case 1: k_solveB<kSolveBMinB[1], 1><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, wx, flags); break;
+    case 2: k_solveB<kSolveBMinB[2], 1><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, wx, flags); break;
+    default: k_solveB<kSolveBMinB[0], 1><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, wx, flags); break;
   }
 }
 void launch_pbfA(const Bufs& b, int k, const float4* velIn, cudaStream_t st) {

@@ -13,6 +13,9 @@ constexpr uint32_t kKindWater = 6u;
 constexpr uint32_t kNbrCap = 64u;      // neighbour-list capacity per particle
 constexpr int kSolveAVariants = 4;      // register-allocation variants (autotuner)
 constexpr int kSolveBVariants = 3;
+// up to this many slots solveA / solveB use four lanes per slot: measured
+// 1.18-1.36x faster substeps at 16k-40k particles, slower from 80k
+constexpr uint32_t kSmallScene = 1u << 16;
 constexpr int kResidChunks = 512;      // per-scene partial sums of the residual
 constexpr int kMaxResid = 129;         // residual slots per scene (iterations + 1)
 constexpr int kFeat = 16;              // network features per particle
@@ -145,7 +148,7 @@ uint32_t scan_tiles(uint32_t cells);
 
 // ---- launchers (solve.cu) ----
 void launch_computeL(const Bufs& b, cudaStream_t st);
-void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, int variant, cudaStream_t st);
+void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, int variant, int lanes, cudaStream_t st);
 void launch_features(const Bufs& b, const float4* velIn, cudaStream_t st);
 void launch_warm_from_net(const Bufs& b, cudaStream_t st);
 void launch_resid_reduce(const Bufs& b, int k, bool warm, cudaStream_t st);
@@ -158,7 +161,7 @@ void mlp_pack(const float* dParams, void* dBlob, cudaStream_t st);
 cudaError_t mlp_forward(const float* dX, uint32_t rows, const void* dBlob, float* dY, float* dZ, int* dErr,
                         cudaStream_t st, bool skipZero = false);
 void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, int flags, int variant,
-                   cudaStream_t st);
+                   int lanes, cudaStream_t st);
 void launch_pbfA(const Bufs& b, int k, const float4* velIn, cudaStream_t st);
 void launch_pbfB(const Bufs& b, int k, const float4* velIn, float4* velOut, cudaStream_t st);
 void launch_xsph(const Bufs& b, const float4* velIn, float4* velOut, cudaStream_t st);

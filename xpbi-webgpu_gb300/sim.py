@@ -275,6 +275,10 @@ class Simulation:
     def set_variants(self, solve_a: int = -1, solve_b: int = -1):
         check(lib().xpbi_set_variants(self._h, solve_a, solve_b))
 
+    def set_lanes(self, lanes: int = 0):
+        """Lanes per particle in solveA / solveB (0: four for small handles)."""
+        check(lib().xpbi_set_lanes(self._h, lanes))
+
     def read_contact_residuals(self, scene: int = 0):
         """Contact residual norms in the slots of read_residuals."""
         out = np.full(256, np.nan)
