@@ -231,12 +231,13 @@ int xpbi_autotune(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t 
 /* Select variants directly (-1 keeps the current one); 0 is the default. */
 int xpbi_set_variants(xpbi_sim* sim, int32_t solve_a, int32_t solve_b);
 
-/* Lanes per particle in solveA / solveB: 1, 4, or 0 (the default) for four
- * when the handle holds at most 65,536 particles. Small scenes leave most of
- * the GPU idle with one thread per particle; four lanes split each
- * particle's neighbour sweep and add their partial sums, which changes the
- * summation order (results agree with one lane to rounding, not bit for
- * bit). The register variants above apply to the one-lane kernels. */
+/* Lanes per particle in solveA / solveB: 1, 2, 4, or 0 (the default) to
+ * choose by the handle's solid particle count (four up to 24,576 solids, two
+ * up to 49,152). Small scenes leave most of the GPU idle with one thread per
+ * particle; several lanes split each particle's neighbour sweep and add their
+ * partial sums, which changes the summation order (results agree with one
+ * lane to rounding, not bit for bit). The register variants above apply to
+ * the one-lane kernels. */
 int xpbi_set_lanes(xpbi_sim* sim, int32_t lanes);
 
 /* ---- solver modes (no counterpart in the reference) ----

@@ -201,7 +201,7 @@ def _clump(xp, sc, oracle, warm, count, material_kind, lanes=0):
     return s0, s1, ref, ref64, p
 
 
-@pytest.mark.parametrize("lanes", [1, 4])
+@pytest.mark.parametrize("lanes", [1, 2, 4])
 def test_crowded_clump_sand(xp, oracle, built_lib, lanes):
     sc = xp.scenes.config_sand_column()
     s0, s1, ref, ref64, p = _clump(xp, sc, oracle, 0, 150, 1, lanes)
@@ -253,8 +253,9 @@ def test_one_lane_per_particle(xp, oracle, built_lib, case):
     compare(s1, ref, ref64, has_pbf=sc["hasWater"], perturbed=perturbed_runs(oracle, sc, s0, xp=xp))
 
 
-def test_four_lanes_on_a_large_handle(xp, oracle, built_lib):
-    """Four lanes forced on a handle above the automatic threshold."""
+@pytest.mark.parametrize("lanes", [2, 4])
+def test_several_lanes_on_a_large_handle(xp, oracle, built_lib, lanes):
+    """Two or four lanes forced on a handle above the automatic thresholds."""
     sc = xp.scenes.config_dam_breach(scale=0.3)
-    s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=5, lanes=4)
+    s0, s1, ref, ref64 = run_pair(xp, oracle, sc, warm=5, lanes=lanes)
     compare(s1, ref, ref64, has_pbf=True, perturbed=perturbed_runs(oracle, sc, s0, xp=xp))

@@ -48,6 +48,7 @@ struct SceneHost {
   int dims[3] = {0, 0, 0};
   xpbi_material mats[kMaxMats];
   uint32_t nMats = 0;
+  uint32_t matCount[kMaxMats] = {0};  // particles per material at creation
   xpbi_params params;
   int iterations = 0, hasWater = 0;
 };
@@ -371,7 +372,17 @@ Schedule schedule(const xpbi_sim* s) {
   sch.keepLam = s->mode != 0 || sch.features;
   sch.varA = s->tuneA;
   sch.varB = s->tuneB;
-  sch.lanes = s->lanesMode ? s->lanesMode : (s->b.N <= kSmallScene ? 4 : 1);
+  if (s->lanesMode) {
+    sch.lanes = s->lanesMode;
+  } else {
+    // the constraint kernels' work is the solid particles (water threads
+    // leave at once): few of them leave the GPU idle with one lane each
+    uint64_t solids = 0;
+    for (const SceneHost& h : s->sc)
+      for (uint32_t m = 0; m < h.nMats; ++m)
+        if (h.mats[m].kind != XPBI_WATER) solids += h.matCount[m];
+    sch.lanes = solids <= kFourLaneSolids ? 4 : (solids <= kTwoLaneSolids ? 2 : 1);
+  }
   for (const SceneHost& h : s->sc) sch.K = std::max(sch.K, h.iterations);
   sch.pbf.assign(sch.K, 0);
   for (const SceneHost& h : s->sc) {
@@ -498,6 +509,7 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
     h.nMats = scenes[i].n_materials;
     std::memset(h.mats, 0, sizeof(h.mats));
     for (uint32_t m = 0; m < h.nMats; ++m) h.mats[m] = scenes[i].materials[m];
+    for (uint32_t k = 0; k < h.n; ++k) ++h.matCount[scenes[i].mat_ids[k]];
     defaultParams(h, h.params);
     N += h.n;
     C += h.numCells;
@@ -1082,8 +1094,9 @@ int xpbi_autotune(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t 
 
 int xpbi_set_lanes(xpbi_sim* sim, int32_t lanes) {
   XPBI_TRY(checkSim(sim));
-  if (lanes != 0 && lanes != 1 && lanes != 4) return fail(XPBI_ERR_INVALID, "lanes must be 0 (by size), 1 or 4");
-  if (lanes == 4 && sim->b.N > (1u << 28)) return fail(XPBI_ERR_INVALID, "four lanes per slot need N <= 2^28");
+  if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4)
+    return fail(XPBI_ERR_INVALID, "lanes must be 0 (by size), 1, 2 or 4");
+  if (lanes > 1 && sim->b.N > (1u << 28)) return fail(XPBI_ERR_INVALID, "several lanes per slot need N <= 2^28");
   sim->lanesMode = lanes;
   return XPBI_OK;
 }

@@ -178,13 +178,13 @@ __device__ __forceinline__ void forNbrs(const Bufs& b, const Ctx& cx, uint32_t i
 
 // Several lanes per slot (small scenes): the G lanes of slot i are
 // consecutive in the warp; lane `lane` visits the list entries k with
-// k % G == lane (each group of four entries is one load, shared by the four
+// k % G == lane (each group of four entries is one load, shared by the
 // lanes), or on the overflow walk every G-th candidate of each row. Each
 // lane accumulates a partial sum; laneSum adds them over the group.
 template <int G, class Gather, class Body>
 __device__ __forceinline__ void forNbrsLanes(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi, uint32_t lane,
                                              Gather&& gather, Body&& body) {
-  static_assert(G == 1 || G == 4, "one or four lanes per slot");
+  static_assert(G == 1 || G == 2 || G == 4, "one, two or four lanes per slot");
   if constexpr (G == 1) {
     (void)lane;
     forNbrs(b, cx, i, xi, gather, body);
@@ -195,8 +195,12 @@ __device__ __forceinline__ void forNbrsLanes(const Bufs& b, const Ctx& cx, uint3
       const uint32_t groups = (cnt + 3u) >> 2;
 #pragma unroll 1
       for (uint32_t q = 0; q < groups; ++q) {
-        const uint32_t e = lane4(__ldg(L + q), lane);
-        if (4u * q + lane < cnt) body(e & ~kWaterBit, (e & kWaterBit) != 0u, gather(e & ~kWaterBit));
+        const uint4 grp = __ldg(L + q);
+#pragma unroll
+        for (uint32_t s = lane; s < 4u; s += G) {
+          const uint32_t e = lane4(grp, s);
+          if (4u * q + s < cnt) body(e & ~kWaterBit, (e & kWaterBit) != 0u, gather(e & ~kWaterBit));
+        }
       }
     } else {
       const SceneDev& S = *cx.scene;
@@ -215,7 +219,10 @@ __device__ __forceinline__ void forNbrsLanes(const Bufs& b, const Ctx& cx, uint3
 
 template <int G>
 __device__ __forceinline__ float laneSum(float v) {
-  if constexpr (G > 1) {
+  if constexpr (G == 2) {
+    const unsigned group = 0x3u << (threadIdx.x & 30u);  // warp lanes 2p, 2p+1
+    v += __shfl_xor_sync(group, v, 1);
+  } else if constexpr (G == 4) {
     const unsigned group = 0xFu << (threadIdx.x & 28u);  // warp lanes 4p .. 4p+3
     v += __shfl_xor_sync(group, v, 1);
     v += __shfl_xor_sync(group, v, 2);
@@ -774,10 +781,14 @@ __global__ void __launch_bounds__(kThreads, kMinB) k_solveB(Bufs b, int k, const
       const uint32_t groups = (cnt + 3u) >> 2;
 #pragma unroll 1
       for (uint32_t q = 0; q < groups; ++q) {
-        const uint32_t e = lane4(__ldg(L + q), lane);
-        if (4u * q + lane < cnt && !(e & kWaterBit)) {
-          const float4* R = Sp + e;
-          body(false, SBData{ldg(R), ldg(R + N), ldg(R + 2 * N), ldg(R + 3 * N)});
+        const uint4 grp = __ldg(L + q);
+#pragma unroll
+        for (uint32_t s = lane; s < 4u; s += G) {
+          const uint32_t e = lane4(grp, s);
+          if (4u * q + s < cnt && !(e & kWaterBit)) {
+            const float4* R = Sp + e;
+            body(false, SBData{ldg(R), ldg(R + N), ldg(R + 2 * N), ldg(R + 3 * N)});
+          }
         }
       }
     } else if (G == 1 && cnt != kNbrOverflow) {
@@ -1058,6 +1069,14 @@ void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, int var
       k_solveA<false, 0, 4><<<grid(threads), kThreads, 0, st>>>(b, k, velIn, flags);
     return;
   }
+  if (lanes == 2) {
+    const uint32_t threads = 2u * b.N;
+    if (flags & kTrackResid)
+      k_solveA<true, 0, 2><<<grid(threads), kThreads, 0, st>>>(b, k, velIn, flags);
+    else
+      k_solveA<false, 0, 2><<<grid(threads), kThreads, 0, st>>>(b, k, velIn, flags);
+    return;
+  }
   switch (variant) {
     case 1: solveAVariant<1>(b, k, velIn, flags, st); break;
     case 2: solveAVariant<2>(b, k, velIn, flags, st); break;
@@ -1080,6 +1099,10 @@ void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bo
   const int wx = writeXc ? 1 : 0;
   if (lanes == 4) {
     k_solveB<0, 4><<<grid(4u * b.N), kThreads, 0, st>>>(b, k, velIn, velOut, wx, flags);
+    return;
+  }
+  if (lanes == 2) {
+    k_solveB<0, 2><<<grid(2u * b.N), kThreads, 0, st>>>(b, k, velIn, velOut, wx, flags);
     return;
   }
   switch (variant) {

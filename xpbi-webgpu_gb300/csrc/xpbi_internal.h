@@ -13,9 +13,11 @@ constexpr uint32_t kKindWater = 6u;
 constexpr uint32_t kNbrCap = 64u;      // neighbour-list capacity per particle
 constexpr int kSolveAVariants = 4;      // register-allocation variants (autotuner)
 constexpr int kSolveBVariants = 3;
-// up to this many slots solveA / solveB use four lanes per slot: measured
-// 1.18-1.36x faster substeps at 16k-40k particles, slower from 80k
-constexpr uint32_t kSmallScene = 1u << 16;
+// Lanes per slot of solveA / solveB by the handle's solid particle count:
+// four up to 24k solids, two up to 48k, else one (measured on sand columns,
+// dam breaches of 8k-120k solids and the 113k-solid snowball)
+constexpr uint64_t kFourLaneSolids = 24576;
+constexpr uint64_t kTwoLaneSolids = 49152;
 constexpr int kResidChunks = 512;      // per-scene partial sums of the residual
 constexpr int kMaxResid = 129;         // residual slots per scene (iterations + 1)
 constexpr int kFeat = 16;              // network features per particle
