@@ -33,7 +33,6 @@ __device__ __forceinline__ F3 f3(float x, float y, float z) { return {x, y, z}; 
 __device__ __forceinline__ F3 operator+(F3 a, F3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
 __device__ __forceinline__ F3 operator-(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 __device__ __forceinline__ F3 operator*(F3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
-__device__ __forceinline__ F3 mulc(F3 a, F3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
 __device__ __forceinline__ float dot3(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ F3 norm3(F3 a) { return a * (1.f / sqrtf(dot3(a, a))); }
 __device__ __forceinline__ F3 mix3(F3 a, F3 b, float t) { return a + (b - a) * t; }
