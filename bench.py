@@ -8,9 +8,10 @@ iterations, dt=1e-4). Inputs are synthetic, seeded lattices.
 
 Arms:
   --impl xpbi       libxpbi (this repo) through its C ABI
-  --impl reference  the reference's algorithm on the host cores: the CPU
-                    oracle port (the WGSL reference path needs a WebGPU
-                    adapter, which neither machine has)
+  --impl reference  the reference's kernels on the host cores: its WGSL
+                    translated mechanically to C++ (oracle/wgsl_ref.py; a
+                    WebGPU adapter exists on neither machine), or the CPU
+                    oracle port where that translation is not built
 """
 from __future__ import annotations
 
@@ -114,19 +115,43 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(sample_scale: float, threads: int, substeps: int = 1):
-    """The oracle port on the host cores over a bounded sample of the
-    workload: one dam-breach scene with its z extent scaled by sample_scale."""
+def cpu_path():
+    """(kind, substep function, description) of the CPU path timed beside
+    the GPU: the reference's own kernels (its WGSL translated to C++ by
+    oracle/wgsl_ref.py) where they are built, else the oracle port."""
     from oracle import oracle as O
+    from oracle import wgsl_ref as W
+    try:
+        if W.build() is not None:
+            W.lib()
+            return "reference", W.substep, "the reference's WGSL kernels translated to C++"
+    except (OSError, RuntimeError) as e:
+        print(f"reference kernels unavailable ({e}); timing the oracle port", file=sys.stderr)
+    return "port", O.substep, "f32 oracle port"
+
+
+def cpu_baseline(sample_scale: float, threads: int, substeps: int = 1, budget_s: float = 0.0):
+    """The CPU path on the host cores over a bounded sample of the workload:
+    one dam-breach scene with its z extent scaled by sample_scale, `substeps`
+    consecutive substeps from rest (with budget_s > 0: stop once that much
+    time has been spent, after at least one). Returns (particle-substeps/s,
+    particles, seconds, substeps run, kind, description)."""
+    from oracle import oracle as O
+    kind, fn, desc = cpu_path()
     xp = importlib.import_module("xpbi-webgpu_gb300")
     sc = xp.scenes.config_dam_breach(seed=0, scale=sample_scale)
     pw, mw = xp.pack_uniforms(sc, xp.params_for(sc))
     st = O.initial_state(sc)
     n = len(sc["positions"])
-    t0 = time.perf_counter()
-    O.substep(pw, mw, st, sc["iterations"], True, sc["pbfIterations"], substeps=substeps, threads=threads)
-    dt = time.perf_counter() - t0
-    return n * substeps / dt, n, dt
+    dt, done = 0.0, 0
+    while done < substeps:
+        t0 = time.perf_counter()
+        st = fn(pw, mw, st, sc["iterations"], True, sc["pbfIterations"], substeps=1, threads=threads)
+        dt += time.perf_counter() - t0
+        done += 1
+        if budget_s > 0 and dt >= budget_s:
+            break
+    return n * done / dt, n, dt, done, kind, desc
 
 
 def host_threads() -> int:
@@ -144,20 +169,20 @@ def run_reference(args, rank: int, world: int):
     # warm-up + timed steps, each one substep of the bounded sample
     for _ in range(args.warmup):
         cpu_baseline(scale, threads)
-    times, n = [], 0
+    times, n, kind, desc = [], 0, "port", ""
     for _ in range(args.steps):
-        v, n, dt = cpu_baseline(scale, threads)
+        v, n, dt, _, kind, desc = cpu_baseline(scale, threads)
         times.append(dt)
     total = sum(times)
     value = n * args.steps / total
     sample = (f"dam-breach scene scaled to {n} particles (z extent x{scale}), one substep "
-              f"(15 XPBI + 4 PBF iterations) per step, f32 oracle port, {threads} threads")
+              f"(15 XPBI + 4 PBF iterations) per step from rest, {desc}, {threads} threads")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference",
             "config": {"workload": args.workload, "solver": "plain", "cpu_sample_particles": n},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -362,10 +387,11 @@ def run_xpbi(args, rank: int, world: int):
            "roofline": roofline, "clocks": clk, "gpu_launches": launches * args.steps,
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}}
     if rank == 0 and not args.no_cpu_baseline:
-        v, n, dt = cpu_baseline(args.cpu_scale, host_threads(), substeps=args.cpu_substeps)
-        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": host_threads(), "kind": "port",
-                               "sample": f"f32 oracle port, {args.cpu_substeps} dam-breach substeps (15 XPBI + "
-                                         f"4 PBF iterations each) of {n} particles from rest, {dt:.1f} s"}
+        v, n, dt, done, kind, desc = cpu_baseline(args.cpu_scale, host_threads(), substeps=args.cpu_substeps,
+                                                  budget_s=args.cpu_budget)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": host_threads(), "kind": kind,
+                               "sample": f"{desc}, {done} dam-breach substeps (15 XPBI + 4 PBF iterations "
+                                         f"each) of {n} particles from rest, {dt:.1f} s"}
     if rank == 0:
         print(json.dumps(out))
     if dist:
@@ -380,6 +406,8 @@ def main():
     ap.add_argument("--impl", default="xpbi", choices=["xpbi", "reference"])
     ap.add_argument("--workload", default="dam_mix4")
     ap.add_argument("--cpu-scale", type=float, default=0.25)
+    ap.add_argument("--cpu-budget", type=float, default=20.0,
+                    help="seconds after which the CPU baseline sample stops (at least one substep)")
     ap.add_argument("--cpu-substeps", type=int, default=30,
                     help="substeps of the CPU baseline sample (about 10 s on 16 cores)")
     ap.add_argument("--profile-substeps", type=int, default=1)

@@ -13,12 +13,16 @@
 // previous index. Everything else is invocation-independent, so the
 // OpenMP-parallel loops give bit-identical results for any thread count.
 //
-// Parity status: the reference has no tests or golden vectors and its WGSL
-// cannot execute here (no WebGPU adapter). The Drucker-Prager return map and
-// the StVK-Hencky energy are pinned against the reference's own NumPy
-// prototype (prototype/xpbi2d.py:93-116) through committed fixtures; the rest
-// is pinned by mathematical known-answer tests only ("parity partially
-// unpinned").
+// Parity status: pinned against the reference's own kernels. Its WGSL cannot
+// execute on a WebGPU adapter here, so oracle/wgsl_ref.py translates that
+// WGSL mechanically into C++ and runs it in sim.js's dispatch order; the f32
+// instantiation below equals it bit for bit (sort, state, multipliers) on
+// every reference demo scene and benchmark config, fresh and developed
+// (tests/test_oracle_vs_reference.py). WGSL leaves determinant()'s
+// evaluation order to the implementation: both use the triple product
+// c0 . (c1 x c2). The Drucker-Prager return map and the StVK-Hencky energy
+// are also checked against the reference's NumPy prototype
+// (prototype/xpbi2d.py:93-116) through committed fixtures.
 //
 // Two instantiations: float (WGSL f32 semantics, the parity oracle) and double
 // (the FP64 error reference of the same substep). Cell coordinates are always

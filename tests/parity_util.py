@@ -15,6 +15,12 @@ substep, and the two results are compared:
     C of a scene at rest. That conditioning, not the kernels, sets MULT_TOL.
 The error of both against the FP64 oracle of the same substep is reported.
 
+Wherever the reference's own kernels are available (oracle/wgsl_ref.py: the
+reference's WGSL translated mechanically to C++ and run on the CPU),
+run_pair also runs them on the same input and requires the f32 oracle to
+equal them bit for bit, so every GPU comparison is against the reference's
+code itself.
+
 Where the reference algorithm itself is not reproducible to REL_TOL in f32 —
 flowing granular material near F = I, where the Hencky strain log(sigma) of
 sigma = 1 + O(1e-4) keeps only ~3 significant digits in f32 and the Jacobi
@@ -68,7 +74,20 @@ def run_pair(xp, O, scene, warm: int = 0, iterations=None, has_water=None, param
         ref64 = O.substep(pw, mw, s0, it, hw, pi, threads=threads, f64=True)
         sim.encode_substep(it, hw)
         s1 = sim.read_state()
+    check_against_reference_kernels(pw, mw, s0, it, hw, pi, ref)
     return s0, s1, ref, ref64
+
+
+def check_against_reference_kernels(pw, mw, s0, it, hw, pi, ref) -> bool:
+    """Requires the f32 oracle's substep `ref` to equal the reference's own
+    kernels bit for bit on the same input; False if they are unavailable."""
+    from oracle import wgsl_ref as W
+    if not W.available():
+        return False
+    wr = W.substep(pw, mw, s0, it, hw, pi)
+    for k in ("pos", "vel", "F", "L", "aux", "sortedIdx", "cellTab"):
+        assert np.array_equal(wr[k], ref[k]), f"oracle differs from the reference's kernels in {k}"
+    return True
 
 
 def perturbed_runs(O, scene, s0, iterations=None, has_water=None, params=None, xp=None, count: int = 3):
