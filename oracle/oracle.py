@@ -52,9 +52,9 @@ def substep(params_words, material_words, state: dict, iterations: int, has_wate
     real = C.c_double if f64 else C.c_float
     n = len(state["pos"])
     nc = int(params_words[7])
-    out = {k: np.ascontiguousarray(state[k], dt).copy() for k in ("pos", "vel", "F", "L", "aux")}
-    if "L" not in state or state["L"] is None:
-        out["L"] = np.zeros((n, 12), dt)
+    out = {k: np.ascontiguousarray(state[k], dt).copy() for k in ("pos", "vel", "F", "aux")}
+    L = state.get("L")
+    out["L"] = np.zeros((n, 12), dt) if L is None else np.ascontiguousarray(L, dt).copy()
     out["sortedIdx"] = np.zeros(n, np.uint32)
     out["cellTab"] = np.zeros(nc, np.uint32)
     pw = np.ascontiguousarray(params_words, np.uint32)
