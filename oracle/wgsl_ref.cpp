@@ -13,7 +13,7 @@
 // Dispatch execution: invocations of kernels with read-modify-write atomics
 // run one at a time in index order (which fixes the order WebGPU leaves
 // open: within a cell the lowest index takes the highest slot); kernels with
-// workgroup barriers run each workgroup's invocations as fibers; every other
+// workgroup barriers run each workgroup's invocations as coroutines; every other
 // kernel runs its invocations in parallel (they write disjoint elements).
 //
 // One extension beside the reference's dispatch order: pbf_iterations >= 0
@@ -40,18 +40,18 @@ const wgsl_ref::Entry* entry(const char* name) {
 
 void dispatch(const wgsl_ref::Entry* e, u32 groups, int threads) {
   const u32 wg = e->wg;
-  if (e->barrier) {
+  if (e->co) {
     if (e->serial) {
       for (u32 w = 0; w < groups; ++w) {
         wgsl_ref::resetWorkgroupVars();
-        runWorkgroup(e->fn, wg, w);
+        runWorkgroup(e->co, wg, w);
       }
       return;
     }
 #pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
     for (long long w = 0; w < (long long)groups; ++w) {
       wgsl_ref::resetWorkgroupVars();
-      runWorkgroup(e->fn, wg, (u32)w);
+      runWorkgroup(e->co, wg, (u32)w);
     }
     return;
   }
@@ -61,7 +61,7 @@ void dispatch(const wgsl_ref::Entry* e, u32 groups, int threads) {
       e->fn(vec3u((u32)g, 0u, 0u), vec3u((u32)(g % wg), 0u, 0u), vec3u((u32)(g / wg), 0u, 0u));
     return;
   }
-#pragma omp parallel for schedule(static) num_threads(threads)
+#pragma omp parallel for schedule(dynamic, 256) num_threads(threads)
   for (long long g = 0; g < total; ++g)
     e->fn(vec3u((u32)g, 0u, 0u), vec3u((u32)(g % wg), 0u, 0u), vec3u((u32)(g / wg), 0u, 0u));
 }

@@ -6,7 +6,7 @@ strings). No WebGPU adapter exists on either machine, so this script
 translates that WGSL mechanically into C++ — the same functions, statements
 and expressions, token by token, with no hand edits — and compiles it with
 oracle/wgsl_rt.h (WGSL types, abstract-float evaluation, builtins, atomics
-in invocation order, workgroup barriers as fibers) and oracle/wgsl_ref.cpp
+in invocation order, workgroup barriers as coroutine suspensions) and oracle/wgsl_ref.cpp
 (the dispatch sequence of web/js/sim.js:220-272) into oracle/_ref/.
 
 Outputs, all under oracle/_ref/ (git-ignored; the generated source travels
@@ -443,16 +443,23 @@ class Translator:
         body_toks = self.t[b0:b1]
         text = self.body(b0, b1)
         entry = any(a[0] == "compute" for a in attrs)
+        barrier = any(x.text == "workgroupBarrier" for x in body_toks)
+        if barrier:
+            if not entry:
+                raise ValueError("workgroupBarrier outside an entry point")
+            # a coroutine: each barrier suspends the invocation
+            text = re.sub(r"\bworkgroupBarrier \( \) ;", "co_await Barrier{} ;", text)
+            text = re.sub(r"\breturn ;", "co_return ;", text)
         if entry:
             names = [builtins.get(k, f"unused{k}_") for k in range(3)]
-            sig = f"static void {name}(vec3u {names[0]}, vec3u {names[1]}, vec3u {names[2]})"
+            rtype = "WgTask" if barrier else "void"
+            sig = f"static {rtype} {name}(vec3u {names[0]}, vec3u {names[1]}, vec3u {names[2]})"
             wg = [a for a in attrs if a[0] == "workgroup_size"]
             if not wg:
                 raise ValueError(f"entry point {name} without workgroup_size")
             wg_expr = " ".join(num(x.text) if x.kind == "num" else ident(x.text) for x in wg[0][1])
             if "," in wg_expr:
                 raise ValueError("multi-dimensional workgroups")
-            barrier = any(x.text == "workgroupBarrier" for x in body_toks)
             # read-modify-write atomics make the invocation order matter: such
             # kernels run their invocations one at a time, in index order
             rmw = any(x.text in _RMW for x in body_toks)
@@ -533,9 +540,10 @@ class Translator:
         parts.append("\n".join(lines))
         parts.append("static void resetWorkgroupVars() {\n" +
                      "".join(f"  {w} = {{}};\n" for w in self.workgroup) + "}")
-        parts.append("struct Entry { const char* name; EntryFn fn; u32 wg; bool barrier; bool serial; };")
+        parts.append("struct Entry { const char* name; EntryFn fn; BarrierFn co; u32 wg; bool serial; };")
         parts.append("static const Entry kEntries[] = {\n" + "".join(
-            f'  {{"{n}", {n}, {wg}, {str(b).lower()}, {str(a).lower()}}},\n' for n, wg, b, a in self.entries) + "};")
+            f'  {{"{n}", {"nullptr" if b else n}, {n if b else "nullptr"}, {wg}, {str(a).lower()}}},\n'
+            for n, wg, b, a in self.entries) + "};")
         parts.append("}  // namespace wgsl_ref")
         return "\n\n".join(parts) + "\n"
 
@@ -572,7 +580,7 @@ def build(force: bool = False) -> str | None:
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in deps):
         return LIB
     tmp = LIB + ".tmp"
-    cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-shared", "-fPIC",
+    cmd = ["g++", "-O3", "-std=c++20", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-shared", "-fPIC",
            "-I", HERE, "-I", OUT, DRIVER, "-o", tmp]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

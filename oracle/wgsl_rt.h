@@ -11,14 +11,14 @@
 //     the same rule, so `sqrt(2.0 / 3.0) * x` rounds the constant once;
 //     abstract integers are C++ int literals;
 //   - builtins with the WGSL names (WGSL spec, "built-in functions");
-//   - atomics for invocations run one at a time, and workgroupBarrier() for
-//     the invocations of one workgroup run as cooperative fibers
-//     (ucontext), so barrier kernels keep their phase semantics.
+//   - atomics for invocations run one at a time, and workgroup barriers for
+//     the invocations of one workgroup run as coroutines, so barrier kernels
+//     keep their phase semantics.
 #pragma once
 
-#include <ucontext.h>
-
 #include <algorithm>
+#include <coroutine>
+#include <exception>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -358,65 +358,43 @@ inline u32 atomicLoad(u32* p) { return *p; }
 inline void atomicStore(u32* p, u32 v) { *p = v; }
 
 // ---------------------------------------------------------------- workgroups
-// The invocations of one workgroup run as fibers on the calling thread; a
-// barrier returns to the scheduler, which resumes every fiber once per round,
-// so no invocation passes a barrier before all have reached it.
+// Entry points with workgroupBarrier() are emitted as coroutines: a barrier
+// is `co_await Barrier{}`. runWorkgroup resumes every invocation of the
+// workgroup once per round, so no invocation passes a barrier before all
+// have reached it (or returned).
 using EntryFn = void (*)(vec3u, vec3u, vec3u);
 
-struct FiberPool {
-  std::vector<ucontext_t> ctx;
-  std::vector<std::vector<char>> stacks;
-  std::vector<char> done;
-  ucontext_t sched;
-  int cur = 0;
-  EntryFn fn = nullptr;
-  u32 wg = 0, wid = 0;
+struct WgTask {
+  struct promise_type {
+    WgTask get_return_object() { return WgTask{std::coroutine_handle<promise_type>::from_promise(*this)}; }
+    std::suspend_always initial_suspend() noexcept { return {}; }
+    std::suspend_always final_suspend() noexcept { return {}; }
+    void return_void() {}
+    void unhandled_exception() { std::terminate(); }
+  };
+  std::coroutine_handle<promise_type> h;
 };
-inline FiberPool*& fiberPool() {
-  static thread_local FiberPool* p = nullptr;
-  return p;
-}
-inline void workgroupBarrier() {
-  FiberPool* fp = fiberPool();
-  swapcontext(&fp->ctx[fp->cur], &fp->sched);
-}
-inline void fiberEntry(int idx) {
-  FiberPool* fp = fiberPool();
-  fp->fn(vec3u(fp->wid * fp->wg + (u32)idx, 0u, 0u), vec3u((u32)idx, 0u, 0u), vec3u(fp->wid, 0u, 0u));
-  fp->done[idx] = 1;
-}
+struct Barrier {
+  bool await_ready() const noexcept { return false; }
+  void await_suspend(std::coroutine_handle<>) const noexcept {}
+  void await_resume() const noexcept {}
+};
+using BarrierFn = WgTask (*)(vec3u, vec3u, vec3u);
+
 // Runs workgroup `wid` of a barrier kernel to completion.
-inline void runWorkgroup(EntryFn fn, u32 wg, u32 wid) {
-  static thread_local FiberPool pool;
-  FiberPool* fp = &pool;
-  fiberPool() = fp;
-  if (fp->ctx.size() < wg) {
-    fp->ctx.resize(wg);
-    fp->stacks.resize(wg);
-    fp->done.resize(wg);
-    for (auto& s : fp->stacks) s.resize(1 << 16);
-  }
-  fp->fn = fn;
-  fp->wg = wg;
-  fp->wid = wid;
-  for (u32 k = 0; k < wg; ++k) {
-    getcontext(&fp->ctx[k]);
-    fp->ctx[k].uc_stack.ss_sp = fp->stacks[k].data();
-    fp->ctx[k].uc_stack.ss_size = fp->stacks[k].size();
-    fp->ctx[k].uc_link = &fp->sched;
-    makecontext(&fp->ctx[k], (void (*)())fiberEntry, 1, (int)k);
-    fp->done[k] = 0;
-  }
+inline void runWorkgroup(BarrierFn fn, u32 wg, u32 wid) {
+  std::vector<std::coroutine_handle<WgTask::promise_type>> inv(wg);
+  for (u32 k = 0; k < wg; ++k) inv[k] = fn(vec3u(wid * wg + k, 0u, 0u), vec3u(k, 0u, 0u), vec3u(wid, 0u, 0u)).h;
   bool any = true;
   while (any) {
     any = false;
-    for (u32 k = 0; k < wg; ++k) {
-      if (fp->done[k]) continue;
-      fp->cur = (int)k;
-      swapcontext(&fp->sched, &fp->ctx[k]);
+    for (auto& h : inv) {
+      if (h.done()) continue;
+      h.resume();
       any = true;
     }
   }
+  for (auto& h : inv) h.destroy();
 }
 
 // ---------------------------------------------------------------- uniform loads
