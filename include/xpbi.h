@@ -212,8 +212,9 @@ int xpbi_render(xpbi_sim* sim, uint32_t scene, const xpbi_camera* cam, uint32_t 
                 uint8_t* rgba_out, void** device_rgba);
 
 /* ---- autotuner (no counterpart in the reference) ----
- * solveA and solveB are built in several register-allocation variants
- * (resident blocks per SM traded against registers). xpbi_autotune runs the
+ * solveA and solveB are built in several launch shapes: block size (64,
+ * 128 or 256 threads) and register allocation (resident blocks per SM traded
+ * against registers). xpbi_autotune runs the
  * substep's preparation (sort, reorder, Bonet-Lok correction) on the current
  * state and times iteration 0 of every variant `repeats` times on this
  * handle's own data, then keeps the fastest of each for the handle (the
@@ -223,8 +224,8 @@ int xpbi_render(xpbi_sim* sim, uint32_t scene, const xpbi_camera* cam, uint32_t 
  * receives the variant indices, ms (may be NULL) the mean time of each
  * variant: XPBI_SOLVEA_VARIANTS entries for solveA, then solveB's. All
  * variants compute the same results; only their speed differs. */
-#define XPBI_SOLVEA_VARIANTS 4
-#define XPBI_SOLVEB_VARIANTS 3
+#define XPBI_SOLVEA_VARIANTS 6
+#define XPBI_SOLVEB_VARIANTS 5
 int xpbi_autotune(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t repeats, int32_t* chosen, float* ms,
                   int32_t cap);
 

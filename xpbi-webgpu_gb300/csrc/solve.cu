@@ -46,15 +46,18 @@ constexpr int kThreads = 128;
 #else
 #define XPBI_LB_COMPUTEL XPBI_LB_DEFAULT
 #endif
-// solveA and solveB are compiled in several register-allocation variants
-// (the minimum resident CTAs per SM asked of the allocator; 0 = its own
-// choice), and xpbi_autotune picks one per handle by timing them on its
-// data. Entry 0 is the default: for solveA 7 CTAs per SM (72 registers, a
-// few spills outside the neighbour loop) measured 15% faster than the
-// allocator's own choice on the 4M-particle dam-breach mix; for solveB the
-// allocator's choice (80 registers) beat every cap.
-constexpr int kSolveAMinB[kSolveAVariants] = {7, 6, 5, 8};
-constexpr int kSolveBMinB[kSolveBVariants] = {0, 7, 5};
+// solveA and solveB are compiled in several launch shapes — the block size
+// and the minimum resident CTAs per SM asked of the register allocator (0 =
+// its own choice) — and xpbi_autotune picks one per handle by timing them on
+// its data. Entry 0 is the default: for solveA 7 CTAs of 128 per SM (72
+// registers, a few spills outside the neighbour loop) measured 15% faster
+// than the allocator's own choice on the 4M-particle dam-breach mix; for
+// solveB the allocator's choice (80 registers) beat every cap. The 64- and
+// 256-thread shapes keep an entry's occupancy with other block sizes.
+constexpr int kSolveAMinB[kSolveAVariants] = {7, 6, 5, 8, 14, 4};
+constexpr int kSolveABlock[kSolveAVariants] = {128, 128, 128, 128, 64, 256};
+constexpr int kSolveBMinB[kSolveBVariants] = {0, 7, 5, 0, 0};
+constexpr int kSolveBBlock[kSolveBVariants] = {128, 128, 128, 64, 256};
 #ifdef XPBI_MINB_PBF
 #define XPBI_LB_PBF __launch_bounds__(kThreads, XPBI_MINB_PBF)
 #else
@@ -462,8 +465,8 @@ __device__ __forceinline__ bool sceneDone(const Bufs& b, uint32_t i) {
 // flags & kMeasureOnly: residual only (the pass after the last iteration).
 // G lanes per slot (G = 4 for small scenes): the lanes split the neighbour
 // sweep, lane 0 finishes the slot.
-template <bool kTrack, int kMinB, int G>
-__global__ void __launch_bounds__(kThreads, kMinB) k_solveA(Bufs b, int k, const float4* __restrict__ velIn,
+template <bool kTrack, int kMinB, int G, int kBlock = kThreads>
+__global__ void __launch_bounds__(kBlock, kMinB) k_solveA(Bufs b, int k, const float4* __restrict__ velIn,
                                                             int flags) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / G, lane = t % G;
@@ -724,8 +727,8 @@ struct SBData {
 //   entering this iteration to rc (the contact residual; 0 for water).
 // flags & kMeasureOnly: the contact residual only, of every solid slot, no
 //   velocity update (the pass after the last iteration).
-template <int kMinB, int G>
-__global__ void __launch_bounds__(kThreads, kMinB) k_solveB(Bufs b, int k, const float4* __restrict__ velIn,
+template <int kMinB, int G, int kBlock = kThreads>
+__global__ void __launch_bounds__(kBlock, kMinB) k_solveB(Bufs b, int k, const float4* __restrict__ velIn,
                                                       float4* __restrict__ velOut, int writeXc, int flags) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / G, lane = t % G;
@@ -1049,6 +1052,7 @@ __global__ void XPBI_LB_UPDATE k_updateF_integrate(Bufs b, const float4* __restr
 }
 
 inline unsigned grid(uint32_t n) { return (unsigned)((n + kThreads - 1) / kThreads); }
+inline unsigned gridOf(uint32_t n, int block) { return (unsigned)((n + (uint32_t)block - 1) / (uint32_t)block); }
 
 }  // namespace
 
@@ -1056,9 +1060,11 @@ void launch_computeL(const Bufs& b, cudaStream_t st) { k_computeL<<<grid(b.N), k
 template <int V>
 void solveAVariant(const Bufs& b, int k, const float4* velIn, int flags, cudaStream_t st) {
   if (flags & kTrackResid)
-    k_solveA<true, kSolveAMinB[V], 1><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, flags);
+    k_solveA<true, kSolveAMinB[V], 1, kSolveABlock[V]><<<gridOf(b.N, kSolveABlock[V]), kSolveABlock[V], 0, st>>>(
+        b, k, velIn, flags);
   else
-    k_solveA<false, kSolveAMinB[V], 1><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, flags);
+    k_solveA<false, kSolveAMinB[V], 1, kSolveABlock[V]><<<gridOf(b.N, kSolveABlock[V]), kSolveABlock[V], 0, st>>>(
+        b, k, velIn, flags);
 }
 void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, int variant, int lanes, cudaStream_t st) {
   if (lanes == 4) {  // small scenes: four lanes per slot, the allocator's register choice
@@ -1081,6 +1087,8 @@ void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, int var
     case 1: solveAVariant<1>(b, k, velIn, flags, st); break;
     case 2: solveAVariant<2>(b, k, velIn, flags, st); break;
     case 3: solveAVariant<3>(b, k, velIn, flags, st); break;
+    case 4: solveAVariant<4>(b, k, velIn, flags, st); break;
+    case 5: solveAVariant<5>(b, k, velIn, flags, st); break;
     default: solveAVariant<0>(b, k, velIn, flags, st); break;
   }
 }
@@ -1094,6 +1102,11 @@ void launch_resid_reduce(const Bufs& b, int k, bool warm, cudaStream_t st) {
   k_resid_final<<<(b.S + 3) / 4, 128, 0, st>>>(b, k, warm ? 1 : 0);
 }
 void launch_keep_lambda(const Bufs& b, cudaStream_t st) { k_keep_lambda<<<grid(b.N), kThreads, 0, st>>>(b); }
+template <int V>
+void solveBVariant(const Bufs& b, int k, const float4* velIn, float4* velOut, int wx, int flags, cudaStream_t st) {
+  k_solveB<kSolveBMinB[V], 1, kSolveBBlock[V]><<<gridOf(b.N, kSolveBBlock[V]), kSolveBBlock[V], 0, st>>>(
+      b, k, velIn, velOut, wx, flags);
+}
 void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, int flags, int variant,
                    int lanes, cudaStream_t st) {
   const int wx = writeXc ? 1 : 0;
@@ -1106,9 +1119,11 @@ void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bo
     return;
   }
   switch (variant) {
-    case 1: k_solveB<kSolveBMinB[1], 1><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, wx, flags); break;
-    case 2: k_solveB<kSolveBMinB[2], 1><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, wx, flags); break;
-    default: k_solveB<kSolveBMinB[0], 1><<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, wx, flags); break;
+    case 1: solveBVariant<1>(b, k, velIn, velOut, wx, flags, st); break;
+    case 2: solveBVariant<2>(b, k, velIn, velOut, wx, flags, st); break;
+    case 3: solveBVariant<3>(b, k, velIn, velOut, wx, flags, st); break;
+    case 4: solveBVariant<4>(b, k, velIn, velOut, wx, flags, st); break;
+    default: solveBVariant<0>(b, k, velIn, velOut, wx, flags, st); break;
   }
 }
 void launch_pbfA(const Bufs& b, int k, const float4* velIn, cudaStream_t st) {

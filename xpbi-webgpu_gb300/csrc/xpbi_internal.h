@@ -11,8 +11,8 @@ constexpr uint32_t kKindSnow = 5u;
 constexpr uint32_t kKindWater = 6u;
 
 constexpr uint32_t kNbrCap = 64u;      // neighbour-list capacity per particle
-constexpr int kSolveAVariants = 4;      // register-allocation variants (autotuner)
-constexpr int kSolveBVariants = 3;
+constexpr int kSolveAVariants = 6;      // launch-shape variants (autotuner): block size, register cap
+constexpr int kSolveBVariants = 5;
 // Lanes per slot of solveA / solveB by the handle's solid particle count:
 // four up to 24k solids, two up to 48k, else one (measured on sand columns,
 // dam breaches of 8k-120k solids and the 113k-solid snowball)

@@ -261,7 +261,7 @@ class Simulation:
         del it
         return out, used.value
 
-    SOLVEA_VARIANTS, SOLVEB_VARIANTS = 4, 3
+    SOLVEA_VARIANTS, SOLVEB_VARIANTS = 6, 5
 
     def autotune(self, iterations: int = -1, has_water: bool = True, repeats: int = 5) -> dict:
         """Time every solveA / solveB variant on this handle's data and keep
