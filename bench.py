@@ -270,7 +270,7 @@ def run_xpbi(args, rank: int, world: int):
     # ---- plain solve (the reference's fixed iteration budget)
     sim, has_water = make_sim(xp, scenes, stream, args.preroll)
     sim.set_solver(0, 0.0, False, False)
-    tuned = sim.autotune(-1, has_water, repeats=5)  # register variants timed on this workload
+    tuned = sim.autotune(-1, has_water, repeats=5)  # launch shapes timed on this workload
     sim.step(args.warmup, -1, has_water)  # graph capture happens here
     sim.synchronize()
     clocks = Clocks(local)
@@ -381,7 +381,9 @@ def run_xpbi(args, rank: int, world: int):
            "config": {"workload": args.workload, "particles_per_gpu": n_total, "scenes": len(scenes),
                       "solver": args.solver, "preroll_substeps": args.preroll,
                       "iterations": [s["iterations"] for s in scenes][:4],
-                      "autotuned_variants": {"solveA": tuned["solveA"], "solveB": tuned["solveB"]},
+                      "autotuned_variants": {"solveA": tuned["solveA"], "solveB": tuned["solveB"],
+                                             "solveA_ms": [round(x, 4) for x in tuned["solveA_ms"]],
+                                             "solveB_ms": [round(x, 4) for x in tuned["solveB_ms"]]},
                       "l2": "inputs larger than L2 (state ~1.3 GB per 4M particles)"},
            "solvers": solvers,
            "roofline": roofline, "clocks": clk, "gpu_launches": launches * args.steps,
