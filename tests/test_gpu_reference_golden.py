@@ -5,7 +5,7 @@ Golden substeps (tests/golden/reference_substeps.npz, made by
 tests/golden/make_reference_golden.py from the reference's WGSL kernels):
 five small scenes covering every material model, contact, walls, the
 collider and both PBF schedules. The GPU starts from each stored input state
-with the same uniforms, runs the same two substeps and must match the stored
+with the same uniforms, runs the same substep and must match the stored
 result under the parity definition of parity_util (sort bit-exact, state
 within 1e-4 relative, with the f32 noise envelope of the oracle where the
 reference algorithm itself is ill-conditioned).
