@@ -54,14 +54,19 @@ def test_tracking_does_not_change_the_solve(xp, built_lib):
         assert np.array_equal(res[0][k], res[1][k]), k
 
 
-def test_zero_network_is_the_previous_multiplier_start(xp, built_lib):
-    """The network predicts an increment over the previous multiplier."""
+@pytest.mark.parametrize("lanes", [0, 1])
+def test_zero_network_is_the_previous_multiplier_start(xp, built_lib, lanes):
+    """The network predicts an increment over the previous multiplier. With
+    one lane per slot the network mode's iteration 0 reads the constraint its
+    features pass evaluated, the previous-multiplier mode evaluates it in
+    solveA: both must give the same bytes."""
     sc = xp.scenes.dam_breach()
     zero = np.zeros(9473, np.float32)
     res = []
     for mode in (2, 1):
         with xp.Simulation(sc) as sim:
             sim.write_params(xp.params_for(sc))
+            sim.set_lanes(lanes)
             sim.set_network(zero)
             sim.set_solver(mode, 0.0, False, False)
             sim.step(5, sc["iterations"], True)

@@ -445,7 +445,11 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
   const int aflags = (sch.reduce ? kTrackResid : 0) | (sch.mode != 0 ? kWarm : 0);
   int in = 0;
   for (int k = 0; k < sch.K; ++k) {
-    launch_solveA(b, k, b.velS[in], aflags, sch.varA, sch.lanes, st);
+    // iteration 0 after a features pass: that pass already evaluated the
+    // constraint at these velocities, with one lane per slot (several lanes
+    // sum in another order, so they evaluate it again)
+    const int stored = k == 0 && sch.features && sch.lanes == 1 ? kStoredC : 0;
+    launch_solveA(b, k, b.velS[in], aflags | stored, sch.varA, sch.lanes, st);
     R.mark(st, "solveA");
     launch_solveB(b, k, b.velS[in], b.velS[in ^ 1], sch.pbf[k] != 0, sch.reduce ? kTrackResid : 0, sch.varB,
                   sch.lanes, st);
@@ -576,6 +580,7 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   A(b.lamPrev, n);
   A(b.lamWarm, n);
   A(b.feat, (size_t)kFeat * n);
+  A(b.cons0, 4 * n);
   A(b.netOut, n);
   A(b.rr, n);
   A(b.c0sq, n);

@@ -437,6 +437,31 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
   return out;
 }
 
+// The iteration-0 constraint of slot i in four float4 planes (plane q of
+// slot i at cons0[q N + i]): the features pass evaluates it at the very
+// velocities iteration 0 starts from, so iteration 0 can read it instead of
+// sweeping the neighbours again.
+__device__ __forceinline__ void storeConstraint(const Bufs& b, uint32_t i, const Constraint& c) {
+  float4* __restrict__ R = b.cons0 + i;
+  const size_t N = b.N;
+  R[0] = make_float4(c.C, c.denom, c.cdot, c.sgrad.x);
+  R[N] = make_float4(c.sgrad.y, c.sgrad.z, c.GL.c[0].x, c.GL.c[0].y);
+  R[2 * N] = make_float4(c.GL.c[0].z, c.GL.c[1].x, c.GL.c[1].y, c.GL.c[1].z);
+  R[3 * N] = make_float4(c.GL.c[2].x, c.GL.c[2].y, c.GL.c[2].z, 0.f);
+}
+__device__ __forceinline__ Constraint loadConstraint(const Bufs& b, uint32_t i) {
+  const float4* __restrict__ R = b.cons0 + i;
+  const size_t N = b.N;
+  const float4 a = R[0], q = R[N], r = R[2 * N], t = R[3 * N];
+  Constraint c;
+  c.C = a.x;
+  c.denom = a.y;
+  c.cdot = a.z;
+  c.sgrad = v3(a.w, q.x, q.y);
+  c.GL = M3{{v3(q.z, q.w, r.x), v3(r.y, r.z, r.w), v3(t.x, t.y, t.z)}};
+  return c;
+}
+
 __device__ __forceinline__ bool sceneDone(const Bufs& b, uint32_t i) {
   const uint32_t s = b.S > 1 ? (uint32_t)b.sceneOf[i] : 0u;
   return b.done[s] != 0;
@@ -463,6 +488,8 @@ __device__ __forceinline__ bool sceneDone(const Bufs& b, uint32_t i) {
 //   replaced by the plain start lambda0 = 0 (the plain solve stays the
 //   fallback). With lambda0 = 0 both updates are the reference's.
 // flags & kMeasureOnly: residual only (the pass after the last iteration).
+// flags & kStoredC (iteration 0, after the features pass): the constraint
+//   is the one the features pass evaluated at the same velocities.
 // G lanes per slot (G = 4 for small scenes): the lanes split the neighbour
 // sweep, lane 0 finishes the slot.
 template <bool kTrack, int kMinB, int G, int kBlock = kThreads>
@@ -488,8 +515,14 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveA(Bufs b, int k, const f
   const uint32_t mi = matOfW(pi.w);
   const float st = b.stateS[i];
   const MatDev m = hardenedMat(cx.mats[mi], st);
-  const Constraint c = evalConstraint<G>(b, cx, i, pi, velIn, m, st, lane);
-  if (G > 1 && lane != 0) return;
+  Constraint c;
+  if ((flags & kStoredC) != 0 && k == 0) {
+    if (G > 1 && lane != 0) return;
+    c = loadConstraint(b, i);
+  } else {
+    c = evalConstraint<G>(b, cx, i, pi, velIn, m, st, lane);
+    if (G > 1 && lane != 0) return;
+  }
   const float g = S.kDamp;
   const float stiff = (1.f + g) * c.denom + S.alphaT;  // d(residual) / d(applied multiplier)
   const float r0 = c.C + g * S.dt * c.cdot;            // residual at lambda = 0
@@ -545,6 +578,7 @@ __global__ void __launch_bounds__(kThreads) k_features(Bufs b, const float4* __r
     const float st = b.stateS[i];
     const MatDev m = hardenedMat(cx.mats[mi], st);
     const Constraint c = evalConstraint(b, cx, i, pi, velIn, m, st);
+    storeConstraint(b, i, c);
     const float aT = S.alphaT;
     f[0] = c.logSigTr.x;
     f[1] = c.logSigTr.y;

@@ -26,6 +26,7 @@ constexpr int kFeat = 16;              // network features per particle
 constexpr int kTrackResid = 1;         // write per-particle residuals
 constexpr int kWarm = 2;               // iteration 0 starts from lamWarm
 constexpr int kMeasureOnly = 4;        // residual only: no multiplier / impulse update
+constexpr int kStoredC = 8;            // iteration 0 reads the constraint the features pass stored
 constexpr uint32_t kNbrOverflow = 0xffffffffu;
 constexpr uint32_t kWaterBit = 0x80000000u;
 
@@ -121,6 +122,7 @@ struct Bufs {
   float* lamPrev;       // [N] the same, carried into this substep's sorted order
   float* lamWarm;       // [N] warm-start multiplier for iteration 0 (sorted)
   float* feat;          // [N][16] network features at iteration 0 (sorted)
+  float4* cons0;        // [4][N] the features pass's iteration-0 constraint: C, denom, cdot, sgrad, GL
   float* netOut;        // [N] network output
   float* rr;            // [N] squared constraint residual of the current iteration
   float* c0sq;          // [N] squared constraint value at the predicted velocities
