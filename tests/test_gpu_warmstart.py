@@ -54,12 +54,12 @@ def test_tracking_does_not_change_the_solve(xp, built_lib):
         assert np.array_equal(res[0][k], res[1][k]), k
 
 
-@pytest.mark.parametrize("lanes", [0, 1])
-def test_zero_network_is_the_previous_multiplier_start(xp, built_lib, lanes):
+@pytest.mark.parametrize("lanes,track", [(0, False), (1, False), (1, True)])
+def test_zero_network_is_the_previous_multiplier_start(xp, built_lib, lanes, track):
     """The network predicts an increment over the previous multiplier. With
-    one lane per slot the network mode's iteration 0 reads the constraint its
-    features pass evaluated, the previous-multiplier mode evaluates it in
-    solveA: both must give the same bytes."""
+    one lane per slot and residual tracking the network mode's iteration 0
+    reads the constraint its features pass evaluated, the previous-multiplier
+    mode evaluates it in solveA: both must give the same bytes."""
     sc = xp.scenes.dam_breach()
     zero = np.zeros(9473, np.float32)
     res = []
@@ -68,7 +68,7 @@ def test_zero_network_is_the_previous_multiplier_start(xp, built_lib, lanes):
             sim.write_params(xp.params_for(sc))
             sim.set_lanes(lanes)
             sim.set_network(zero)
-            sim.set_solver(mode, 0.0, False, False)
+            sim.set_solver(mode, 0.0, track, False)
             sim.step(5, sc["iterations"], True)
             res.append(sim.read_state())
     for k in ("pos", "vel", "F", "sortedIdx"):

@@ -443,6 +443,9 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
     cudaMemsetAsync(b.itersUsed, 0, sizeof(int) * b.S, st);
   }
   const int aflags = (sch.reduce ? kTrackResid : 0) | (sch.mode != 0 ? kWarm : 0);
+  // solveA(k) records the scenes' largest solid displacement in slot k & 1,
+  // solveB(k) clears the other slot for the next iteration
+  cudaMemsetAsync(b.solidDisp, 0, sizeof(uint32_t) * 2 * b.S, st);
   int in = 0;
   for (int k = 0; k < sch.K; ++k) {
     // iteration 0 after a features pass: that pass already evaluated the
@@ -585,6 +588,7 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   A(b.rr, n);
   A(b.c0sq, n);
   A(b.rc, n);
+  A(b.solidDisp, 2 * (size_t)nScenes);
   A(b.residPart, (size_t)nScenes * kResidChunks * 3);
   A(b.resid, (size_t)nScenes * kMaxResid);
   A(b.residC, (size_t)nScenes * kMaxResid);
@@ -1058,6 +1062,7 @@ int xpbi_autotune(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t 
     launch_reorder(b, false, st);
     launch_computeL(b, st);
     cudaMemsetAsync(b.done, 0, sizeof(int) * b.S, st);  // no scene counts as converged here
+    cudaMemsetAsync(b.solidDisp, 0, sizeof(uint32_t) * 2 * b.S, st);
     // iteration 0 of each variant from lambda = 0, then solveB on its record
     for (int v = 0; v < kSolveAVariants; ++v)
       t[v] = timed([&] { launch_solveA(b, 0, b.velS[0], 0, v, 1, st); });

@@ -467,6 +467,19 @@ __device__ __forceinline__ bool sceneDone(const Bufs& b, uint32_t i) {
   return b.done[s] != 0;
 }
 
+// Largest solid displacement dt |v| per scene entering iteration k (slot
+// k & 1 of solidDisp, cleared by solveB(k - 1) or at the substep's start).
+// Called by every thread of the warp before any of them leaves: the lanes of
+// one scene combine their values and one of them raises the slot.
+__device__ __forceinline__ void recordSolidDisp(const Bufs& b, uint32_t i, int k, float d) {
+  const unsigned act = __activemask();
+  const uint32_t sc = b.S > 1 ? (uint32_t)b.sceneOf[i] : 0u;
+  const unsigned peers = b.S > 1 ? __match_any_sync(act, sc) : act;
+  const unsigned mx = __reduce_max_sync(peers, __float_as_uint(d));  // d >= 0: bits order like values
+  if ((threadIdx.x & 31u) == (unsigned)(__ffs(peers) - 1) && mx != 0u)
+    atomicMax(b.solidDisp + (size_t)(k & 1) * b.S + sc, mx);
+}
+
 // Inelastic constraint pass A (simkernels.js:248-309).
 //
 // flags & kTrackResid: writes r^2 for the residual of the state entering
@@ -488,8 +501,9 @@ __device__ __forceinline__ bool sceneDone(const Bufs& b, uint32_t i) {
 //   replaced by the plain start lambda0 = 0 (the plain solve stays the
 //   fallback). With lambda0 = 0 both updates are the reference's.
 // flags & kMeasureOnly: residual only (the pass after the last iteration).
-// flags & kStoredC (iteration 0, after the features pass): the constraint
-//   is the one the features pass evaluated at the same velocities.
+// flags & kStoredC (iteration 0, after the features pass; tracked instances):
+//   the constraint is the one the features pass evaluated at the same
+//   velocities. The plain instances keep their registers for the sweep.
 // G lanes per slot (G = 4 for small scenes): the lanes split the neighbour
 // sweep, lane 0 finishes the slot.
 template <bool kTrack, int kMinB, int G, int kBlock = kThreads>
@@ -501,10 +515,11 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveA(Bufs b, int k, const f
   const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
   constexpr bool track = kTrack;
-  const bool measure = (flags & kMeasureOnly) != 0;
+  const bool measure = kTrack && (flags & kMeasureOnly) != 0;  // measure passes are tracked ones
   const bool warm0 = (flags & kWarm) != 0 && k == 0;
   const float4 pi = b.posS[i];
   const bool active = measure || (k < S.iterations && !sceneDone(b, i));
+  recordSolidDisp(b, i, k, active && !waterW(pi.w) && lane == 0 ? S.dt * length(xyz(velIn[i])) : 0.f);
   if (!active || waterW(pi.w)) {  // water: its record is never read
     if (track && lane == 0) {
       b.rr[i] = 0.f;
@@ -516,7 +531,7 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveA(Bufs b, int k, const f
   const float st = b.stateS[i];
   const MatDev m = hardenedMat(cx.mats[mi], st);
   Constraint c;
-  if ((flags & kStoredC) != 0 && k == 0) {
+  if (kTrack && (flags & kStoredC) != 0 && k == 0) {  // the tracked (solver-mode) instances only
     if (G > 1 && lane != 0) return;
     c = loadConstraint(b, i);
   } else {
@@ -538,11 +553,14 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveA(Bufs b, int k, const f
     b.rr[i] = r * r;
     if (k == 0) b.c0sq[i] = r0 * r0;
   }
-  if (measure) return;
   // an inactive constraint still takes part in the contact pass
   const V3 xi = xyz(pi);
   const V3 xci = xi + S.dt * xyz(velIn[i]);
   const float mass = cx.mats[mi].mass;
+  if (measure) {  // the contact residual of these velocities, no impulse
+    storeSp(b, i, mzero(), splat(0.f), xi, xci, mass);
+    return;
+  }
   if (c.C == 0.f) {
     if (k == 0) b.lam[i] = lam0;
     storeSp(b, i, mzero(), splat(0.f), xi, xci, mass);
@@ -750,7 +768,7 @@ __device__ __forceinline__ V3 applyBoundary(const SceneDev& S, V3 xcIn, V3 vIn, 
 }
 
 struct SBData {
-  float4 r0, r1, r2, r3;  // a neighbour's solveB record
+  float4 r0, r1, r2;  // a neighbour's dlam G L columns with its position in .w (the record's first planes)
 };
 
 // ---------------------------------------------------------------- solveB
@@ -766,6 +784,7 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveB(Bufs b, int k, const f
                                                       float4* __restrict__ velOut, int writeXc, int flags) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / G, lane = t % G;
+  if (t < b.S) b.solidDisp[(size_t)((k + 1) & 1) * b.S + t] = 0u;  // the next iteration's slot
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
@@ -796,17 +815,31 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveB(Bufs b, int k, const f
     const V3 xci = xi + S.dt * xyz(vi4);
     const float minD = S.minD;
     const float massI = m.mass;
-    auto body = [&](bool water, const SBData& d) {
+    // A neighbour can be within minD of x_i + dt v_i at the predicted
+    // positions only if |x_b - x_i| < minD + dt |v_i| + dt |v_b|, and dt |v_b|
+    // is at most the scene's largest solid displacement this iteration
+    // (recorded by solveA): farther neighbours skip the contact test and the
+    // load of their predicted position. 1% of slack covers the rounding of
+    // the predicted positions and of the bound; the test on the pairs that
+    // remain is unchanged, so the result is too.
+    const float reach = (minD + S.dt * length(xyz(vi4)) +
+                         __uint_as_float(__ldg(b.solidDisp + (size_t)(k & 1) * b.S + (cx.scene - b.scenes)))) *
+                        1.01f;
+    const float reach2 = reach * reach;
+    auto body = [&](uint32_t j, bool water, const SBData& d) {
       if (water) return;
       const V3 pb = v3(d.r0.w, d.r1.w, d.r2.w);
       const M3 Sb = {{xyz(d.r0), xyz(d.r1), xyz(d.r2)}};
-      dv = dv + Vi * mul(Sb, gradWFast(S, pb - xi));
-      const V3 dxc = xci - xyz(d.r3);
+      const V3 dxp = pb - xi;
+      dv = dv + Vi * mul(Sb, gradWFast(S, dxp));
+      if (!(dot(dxp, dxp) < reach2)) return;
+      const float4 r3 = ldg(Sp + 3 * b.N + j);
+      const V3 dxc = xci - xyz(r3);
       const float d2 = dot(dxc, dxc);
       if (d2 < minD * minD && d2 > 1e-18f) {
         const float rinv = rsqrtf(d2);
         const float dist = d2 * rinv;
-        const float mb = d.r3.w;
+        const float mb = r3.w;
         const float w = mb / (massI + mb);
         corr = corr + dxc * (rinv * ((minD - dist) * w));
       }
@@ -824,7 +857,7 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveB(Bufs b, int k, const f
           const uint32_t e = lane4(grp, s);
           if (4u * q + s < cnt && !(e & kWaterBit)) {
             const float4* R = Sp + e;
-            body(false, SBData{ldg(R), ldg(R + N), ldg(R + 2 * N), ldg(R + 3 * N)});
+            body(e, false, SBData{ldg(R), ldg(R + N), ldg(R + 2 * N)});
           }
         }
       }
@@ -834,17 +867,16 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveB(Bufs b, int k, const f
                     [&](uint32_t e) {
                       SBData d;
                       if (e & kWaterBit) {
-                        d.r0 = d.r1 = d.r2 = d.r3 = make_float4(0.f, 0.f, 0.f, 0.f);
+                        d.r0 = d.r1 = d.r2 = make_float4(0.f, 0.f, 0.f, 0.f);
                       } else {
                         const float4* R = Sp + e;
                         d.r0 = ldg(R);
                         d.r1 = ldg(R + N);
                         d.r2 = ldg(R + 2 * N);
-                        d.r3 = ldg(R + 3 * N);
                       }
                       return d;
                     },
-                    [&](uint32_t, bool water, const SBData& d) { body(water, d); });
+                    [&](uint32_t j, bool water, const SBData& d) { body(j, water, d); });
     } else {
       forRows(S, b.cellStart, xi, [&](uint32_t beg, uint32_t end) {
 #pragma unroll 1
@@ -854,7 +886,7 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveB(Bufs b, int k, const f
           const V3 d = xi - xyz(pj);
           if (dot(d, d) < S.support2 && !waterW(pj.w)) {
             const float4* R = Sp + j;
-            body(false, SBData{ldg(R), ldg(R + N), ldg(R + 2 * N), ldg(R + 3 * N)});
+            body(j, false, SBData{ldg(R), ldg(R + N), ldg(R + 2 * N)});
           }
         }
       });

@@ -127,6 +127,7 @@ struct Bufs {
   float* rr;            // [N] squared constraint residual of the current iteration
   float* c0sq;          // [N] squared constraint value at the predicted velocities
   float* rc;            // [N] squared contact correction of the current iteration
+  uint32_t* solidDisp;  // [2][S] float bits: largest dt |v| of a scene's solids entering iteration k (slot k & 1)
   double* residPart;    // [S][kResidChunks][3] partial sums
   double* resid;        // [S][kMaxResid] residual norm^2 per iteration (last slot: after the last)
   double* residC;       // [S][kMaxResid] contact residual norm^2, same slots
