@@ -158,13 +158,25 @@ __device__ __forceinline__ void forList(const uint32_t* __restrict__ list, uint3
 
 __device__ __forceinline__ uint32_t* listOf(uint32_t* base, uint32_t i) { return base + (size_t)i * kNbrCap; }
 
+// Keeps every recorded neighbour.
+struct KeepAll {
+  __device__ __forceinline__ bool operator()(uint32_t) const { return true; }
+};
+
 // In-support neighbours of slot i in stencil order: body(j, jIsWater, data).
-template <class Gather, class Body>
+// keep(entry) (index | water bit) false: the body will ignore that neighbour,
+// so its data is not loaded (the body receives a zero-initialised value).
+template <class Gather, class Body, class Keep = KeepAll>
 __device__ __forceinline__ void forNbrs(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi, Gather&& gather,
-                                        Body&& body) {
+                                        Body&& body, Keep keep = Keep{}) {
   const uint32_t cnt = b.nbrCount[i];
   if (cnt != kNbrOverflow) {
-    forList(listOf(b.nbr, i), cnt, gather, body);
+    forList<true>(listOf(b.nbr, i), cnt,
+                  [&](uint32_t e) {
+                    using T = decltype(gather(0u));
+                    return keep(e) ? gather(e & ~kWaterBit) : T{};
+                  },
+                  body);
   } else {
     const SceneDev& S = *cx.scene;
     forRows(S, b.cellStart, xi, [&](uint32_t beg, uint32_t end) {
@@ -184,13 +196,13 @@ __device__ __forceinline__ void forNbrs(const Bufs& b, const Ctx& cx, uint32_t i
 // k % G == lane (each group of four entries is one load, shared by the
 // lanes), or on the overflow walk every G-th candidate of each row. Each
 // lane accumulates a partial sum; laneSum adds them over the group.
-template <int G, class Gather, class Body>
+template <int G, class Gather, class Body, class Keep = KeepAll>
 __device__ __forceinline__ void forNbrsLanes(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi, uint32_t lane,
-                                             Gather&& gather, Body&& body) {
+                                             Gather&& gather, Body&& body, Keep keep = Keep{}) {
   static_assert(G == 1 || G == 2 || G == 4, "one, two or four lanes per slot");
   if constexpr (G == 1) {
     (void)lane;
-    forNbrs(b, cx, i, xi, gather, body);
+    forNbrs(b, cx, i, xi, gather, body, keep);
   } else {
     const uint32_t cnt = b.nbrCount[i];
     if (cnt != kNbrOverflow) {
@@ -202,7 +214,7 @@ __device__ __forceinline__ void forNbrsLanes(const Bufs& b, const Ctx& cx, uint3
 #pragma unroll
         for (uint32_t s = lane; s < 4u; s += G) {
           const uint32_t e = lane4(grp, s);
-          if (4u * q + s < cnt) body(e & ~kWaterBit, (e & kWaterBit) != 0u, gather(e & ~kWaterBit));
+          if (4u * q + s < cnt && keep(e)) body(e & ~kWaterBit, (e & kWaterBit) != 0u, gather(e & ~kWaterBit));
         }
       }
     } else {
@@ -308,6 +320,11 @@ __device__ __forceinline__ void storeSp(const Bufs& b, uint32_t i, const M3& m, 
   b.SpSelf[i] = make_float4(self.x, self.y, self.z, 0.f);
 }
 
+// Solid neighbours only: water entries are skipped before their data loads.
+struct SolidOnly {
+  __device__ __forceinline__ bool operator()(uint32_t e) const { return (e & kWaterBit) == 0u; }
+};
+
 // velocityGradient (simkernels.js:224-245) over the neighbour list.
 __device__ __forceinline__ M3 velocityGradient(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi, V3 vi,
                                                const float4* __restrict__ velIn) {
@@ -315,13 +332,15 @@ __device__ __forceinline__ M3 velocityGradient(const Bufs& b, const Ctx& cx, uin
   const float4* __restrict__ posS = b.posS;
   // sum dv_b (L g_b)^T = (sum dv_b g_b^T) L^T: L applied once, after the loop
   M3 A = mzero();
-  forNbrs(b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
-          [&](uint32_t, bool water, const PV& d) {
-            if (water) return;
-            const V3 g = gradWFast(S, xi - xyz(d.p));
-            const V3 dv = (xyz(d.v) - vi) * d.v.w;
-            A = madd(A, M3{{dv * g.x, dv * g.y, dv * g.z}});
-          });
+  forNbrs(
+      b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
+      [&](uint32_t, bool water, const PV& d) {
+        if (water) return;
+        const V3 g = gradWFast(S, xi - xyz(d.p));
+        const V3 dv = (xyz(d.v) - vi) * d.v.w;
+        A = madd(A, M3{{dv * g.x, dv * g.y, dv * g.z}});
+      },
+      SolidOnly{});
   return mul(A, transpose(loadM(b.L, b.N, i)));
 }
 
@@ -367,7 +386,8 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
   M3 A = mzero();
   V3 sg = splat(0.f);
   float p00 = 0.f, p11 = 0.f, p22 = 0.f, p01 = 0.f, p02 = 0.f, p12 = 0.f, cnt = 0.f;
-  forNbrsLanes<NL>(b, cx, i, xi, lane, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
+  forNbrsLanes<NL>(
+      b, cx, i, xi, lane, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
           [&](uint32_t, bool water, const PV& d) {
             if (water) return;
             const V3 g = gradWFast(S, xi - xyz(d.p));
@@ -384,7 +404,8 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
             p02 += cg.x * g.z;
             p12 += cg.y * g.z;
             cnt += 1.f;
-          });
+          },
+      SolidOnly{});
   if constexpr (NL > 1) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) A.c[c] = laneSum<NL>(A.c[c]);
@@ -1071,12 +1092,14 @@ __global__ void XPBI_LB_UPDATE k_xsph(Bufs b, const float4* __restrict__ velIn,
   const V3 vi = xyz(vi4);
   const bool iWater = waterW(pi.w);
   V3 acc = splat(0.f);
-  forNbrs(b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
-          [&](uint32_t, bool jWater, const PV& d) {
-            if (jWater != iWater) return;
-            const V3 dxv = xi - xyz(d.p);
-            acc = acc + d.v.w * (xyz(d.v) - vi) * kernelWFast(S, dot(dxv, dxv));
-          });
+  forNbrs(
+      b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
+      [&](uint32_t, bool jWater, const PV& d) {
+        if (jWater != iWater) return;
+        const V3 dxv = xi - xyz(d.p);
+        acc = acc + d.v.w * (xyz(d.v) - vi) * kernelWFast(S, dot(dxv, dxv));
+      },
+      [iWater](uint32_t e) { return ((e & kWaterBit) != 0u) == iWater; });  // same phase only
   float c = S.xsphC;
   if (iWater) c = S.xsphC * 10.f;
   const V3 v = vi + c * acc;
