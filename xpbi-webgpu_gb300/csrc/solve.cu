@@ -260,7 +260,9 @@ __device__ __forceinline__ uint32_t recordCandidates(const SceneDev& S, const ui
     for (uint32_t j = beg; j < end; ++j) {
       uint32_t e;
       const bool ok = test(j, e) && j != i;
-      if (ok && cnt < kNbrCap) out[cnt] = e;
+      // past the capacity the last slot is overwritten: such a list is
+      // marked as overflowed and never read
+      if (ok) out[min(cnt, kNbrCap - 1u)] = e;
       cnt += ok ? 1u : 0u;
     }
   });
@@ -282,7 +284,7 @@ __global__ void XPBI_LB_COMPUTEL k_computeL(Bufs b) {
   const uint32_t cnt = recordCandidates(S, b.cellStart, xi, i, listOf(b.nbr, i), [&](uint32_t j, uint32_t& e) {
     const float4 p = ldg(posS + j);
     const V3 d = xi - xyz(p);
-    e = j | (waterW(p.w) ? kWaterBit : 0u);
+    e = j | (__float_as_uint(p.w) & kWaterBit);  // the water flag is the sign bit of pos.w
     return dot(d, d) < s2;
   });
   b.nbrCount[i] = cnt <= kNbrCap ? cnt : kNbrOverflow;
@@ -973,13 +975,22 @@ __global__ void XPBI_LB_PBF k_pbfA(Bufs b, int k) {
   }
   const V3 xci = xyz(xcS[i]);
   const float s2 = S.support2;
-  const uint32_t cnt = recordCandidates(S, b.cellStart, xyz(pi), i, listOf(b.nbrP, i), [&](uint32_t j, uint32_t& e) {
-    const float4 c = ldg(xcS + j);
-    const V3 d = xci - xyz(c);
-    const bool jWater = waterW(c.w);
-    e = j | (jWater ? kWaterBit : 0u);
-    return (iWater || jWater) && dot(d, d) < s2;
-  });
+  // the water flag is the sign bit of xc.w (the sorted pos.w)
+  const uint32_t cnt =
+      iWater ? recordCandidates(S, b.cellStart, xyz(pi), i, listOf(b.nbrP, i),
+                                [&](uint32_t j, uint32_t& e) {  // water pairs with everything
+                                  const float4 c = ldg(xcS + j);
+                                  const V3 d = xci - xyz(c);
+                                  e = j | (__float_as_uint(c.w) & kWaterBit);
+                                  return dot(d, d) < s2;
+                                })
+             : recordCandidates(S, b.cellStart, xyz(pi), i, listOf(b.nbrP, i),
+                                [&](uint32_t j, uint32_t& e) {  // a solid with water only
+                                  const float4 c = ldg(xcS + j);
+                                  const V3 d = xci - xyz(c);
+                                  e = j | kWaterBit;
+                                  return waterW(c.w) && dot(d, d) < s2;
+                                });
   const uint32_t stored = cnt <= kNbrCap ? cnt : kNbrOverflow;
   b.nbrPCount[i] = stored;
   if (!iWater) {
