@@ -237,6 +237,16 @@ void buildSceneDev(const SceneHost& s, uint32_t sceneIdx, SceneDev& d, MatDev* m
     M.mass = wf(q, 13);
     M.massPerDensity = M.density != 0.f ? M.mass / M.density : 0.f;
   }
+  // PBF pairs weight by the water particle's mass / density; with one water
+  // material it is a scene constant
+  d.waterMpd = 0.f;
+  int nWater = 0;
+  for (uint32_t i = 0; i < s.nMats && i < (uint32_t)kMaxMats; ++i)
+    if (md[i].kind == kKindWater) {
+      ++nWater;
+      d.waterMpd = md[i].massPerDensity;
+    }
+  if (nWater != 1) d.waterMpd = 0.f;
 }
 
 int validateScene(const xpbi_scene_desc* d) {
@@ -579,6 +589,7 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   A(b.nbrP, (size_t)kNbrCap * n);
   A(b.nbrPCount, n);
   A(b.xc, n);
+  A(b.pbfRec, n);
   A(b.lamOut, n);
   A(b.lamPrev, n);
   A(b.lamWarm, n);

@@ -970,6 +970,7 @@ __global__ void XPBI_LB_PBF k_pbfA(Bufs b, int k) {
     if (!near) {
       b.nbrPCount[i] = 0u;
       b.pbfLam[i] = 0.f;
+      b.pbfRec[i] = make_float4(0.f, 0.f, 0.f, 0.f);  // no PBF pair reads it
       return;
     }
   }
@@ -995,6 +996,7 @@ __global__ void XPBI_LB_PBF k_pbfA(Bufs b, int k) {
   b.nbrPCount[i] = stored;
   if (!iWater) {
     b.pbfLam[i] = 0.f;
+    b.pbfRec[i] = make_float4(xci.x, xci.y, xci.z, 0.f);
     return;
   }
   const MatDev& m = cx.mats[matOfW(pi.w)];
@@ -1026,7 +1028,9 @@ __global__ void XPBI_LB_PBF k_pbfA(Bufs b, int k) {
     });
   }
   const float C = fmaxf(rho * invRho0 - 1.f, 0.f);
-  b.pbfLam[i] = -C / (grad2 + dot(gradSum, gradSum) + S.pbfEps);
+  const float lam = -C / (grad2 + dot(gradSum, gradSum) + S.pbfEps);
+  b.pbfLam[i] = lam;
+  b.pbfRec[i] = make_float4(xci.x, xci.y, xci.z, lam);
 }
 
 struct PBData {
@@ -1058,17 +1062,26 @@ __global__ void XPBI_LB_PBF k_pbfB(Bufs b, int k, const float4* __restrict__ vel
   const bool iWater = waterW(pi.w);
   const MatDev& mWi = cx.mats[mi];
   auto gather = [&](uint32_t j) { return PBData{ldg(xcS + j), ldg(lam + j)}; };
-  auto body = [&](uint32_t, bool jWater, const PBData& d) {
-    const V3 dxv = xci - xyz(d.c);
+  auto term = [&](V3 xcb, float lb, float mpd) {
+    const V3 dxv = xci - xcb;
     const float r2 = dot(dxv, dxv);
-    const MatDev& mw = jWater ? cx.mats[matOfW(d.c.w)] : mWi;  // a water material
     const float x = poly6Fast(S, r2) * S.invW0;
     const float x2 = x * x;
     const float sCorr = -S.sCorrK * (x2 * x2);
-    dp = dp + (li + d.lb + sCorr) * spikyGradFast(S, dxv, r2) * mw.massPerDensity;
+    dp = dp + (li + lb + sCorr) * spikyGradFast(S, dxv, r2) * mpd;
+  };
+  auto body = [&](uint32_t, bool jWater, const PBData& d) {
+    const MatDev& mw = jWater ? cx.mats[matOfW(d.c.w)] : mWi;  // a water material
+    term(xyz(d.c), d.lb, mw.massPerDensity);
   };
   const uint32_t cnt = b.nbrPCount[i];
-  if (cnt != kNbrOverflow) {
+  if (cnt != kNbrOverflow && S.waterMpd > 0.f) {
+    // one water material: every pair weighs by its mass / density, and one
+    // gather of pbfA's record (predicted position, multiplier) serves a pair
+    const float mpd = S.waterMpd;
+    forList(listOf(b.nbrP, i), cnt, [&](uint32_t j) { return ldg(b.pbfRec + j); },
+            [&](uint32_t, bool, const float4& r) { term(xyz(r), r.w, mpd); });
+  } else if (cnt != kNbrOverflow) {
     forList(listOf(b.nbrP, i), cnt, gather, body);
   } else {
     forRows(S, b.cellStart, xyz(pi), [&](uint32_t beg, uint32_t end) {

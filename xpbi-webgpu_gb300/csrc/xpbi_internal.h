@@ -73,6 +73,7 @@ struct SceneDev {
   int hasWater;
   float residTol;           // early stop at |r_k| <= residTol |C(v_pred)|; <= 0: never
   float residTolC;          // ... and |contact_k| <= residTolC |contact_0|
+  float waterMpd;           // mass / density of the scene's one water material; 0: none or several
 };
 
 struct MatDev {
@@ -117,6 +118,7 @@ struct Bufs {
   uint32_t* nbrP;       // [N][kNbrCap] predicted-position neighbours of the current PBF pass
   uint32_t* nbrPCount;  // [N]
   float4* xc;           // [N] predicted positions x + dt v of the current PBF pass, w = pos.w
+  float4* pbfRec;       // [N] the same predicted position with the pass's PBF multiplier in .w (written by pbfA)
   // solver instrumentation and warm start
   float* lamOut;        // [N] final multiplier of the last substep, current order
   float* lamPrev;       // [N] the same, carried into this substep's sorted order
