@@ -30,9 +30,10 @@ if the GPU is no further from the f64 oracle than NOISE_FACTOR times the f32
 noise envelope of the substep (and no further from the f32 oracle than that
 plus the envelope). The envelope is the largest distance from the f64 oracle
 over the f32 oracle run on the input and, where the case supplies them, on
-inputs whose velocities carry a 1e-7 relative perturbation: one f32 run is a
-single sample of rounding noise that such a substep amplifies, and the GPU's
-own (equally valid) rounding is another sample. The f64 response of such a
+inputs whose velocities (for crowded clumps, positions and F as well) carry
+a 1e-7 relative perturbation: one f32 run is a single sample of rounding
+noise that such a substep amplifies, and the GPU's own (equally valid)
+rounding is another sample. The f64 response of such a
 state to a 1e-7 input perturbation is 1e-7, so the spread is f32 rounding,
 not physics.
 """
@@ -90,10 +91,15 @@ def check_against_reference_kernels(pw, mw, s0, it, hw, pi, ref) -> bool:
     return True
 
 
-def perturbed_runs(O, scene, s0, iterations=None, has_water=None, params=None, xp=None, count: int = 3):
+def perturbed_runs(O, scene, s0, iterations=None, has_water=None, params=None, xp=None, count: int = 3,
+                   positions: bool = False):
     """f32 oracle runs of the substep run_pair checked, from inputs whose
-    velocities carry a seeded 1e-7 relative perturbation (the noise envelope
-    of compare); returns a callable so the runs happen only when needed."""
+    velocities (and with `positions`, positions and F too) carry a seeded
+    1e-7 relative perturbation (the noise envelope of compare); returns a
+    callable so the runs happen only when needed. Position perturbations
+    suit states driven by overlaps (crowded clumps), whose response to
+    rounding is through the contact distances; a sample whose perturbation
+    moved a particle across a cell boundary is left out by compare."""
     p = xp.params_for(scene) if params is None else params
     it = scene["iterations"] if iterations is None else iterations
     hw = scene["hasWater"] if has_water is None else has_water
@@ -109,6 +115,15 @@ def perturbed_runs(O, scene, s0, iterations=None, has_water=None, params=None, x
             v = s0["vel"].copy()
             v[:, :3] *= (1.0 + 1e-7 * rng.uniform(-1.0, 1.0, size=(len(v), 3))).astype(np.float32)
             s["vel"] = v
+            if positions:
+                x = s0["pos"].copy()
+                x[:, :3] *= (1.0 + 1e-7 * rng.uniform(-1.0, 1.0, size=(len(x), 3))).astype(np.float32)
+                s["pos"] = x
+                # F too: V^n = V0 det F weighs every neighbour sum, the
+                # Bonet-Lok correction's included
+                F = s0["F"].copy()
+                F *= (1.0 + 1e-7 * rng.uniform(-1.0, 1.0, size=F.shape)).astype(np.float32)
+                s["F"] = F
             out.append(O.substep(pw, mw, s, it, hw, pi))
         return out
     return runs
@@ -153,7 +168,10 @@ def compare(s1, ref, ref64=None, has_pbf: bool = False, perturbed=None) -> dict:
         env = report[f + "_f32oracle_vs_f64"]
         if perturbed is not None:
             if "_pert" not in report:
-                report["_pert"] = [_split(p) for p in perturbed()]
+                # samples sorted like the reference only (a perturbation that
+                # moved a particle into another cell permutes the arrays)
+                report["_pert"] = [_split(p) for p in perturbed()
+                                   if np.array_equal(p["sortedIdx"], ref["sortedIdx"])]
             for p in report["_pert"]:
                 env = max(env, rel(p[f], c_[f]))
             report[f + "_f32_envelope"] = env

@@ -205,13 +205,14 @@ def _clump(xp, sc, oracle, warm, count, material_kind, lanes=0):
 def test_crowded_clump_sand(xp, oracle, built_lib, lanes):
     sc = xp.scenes.config_sand_column()
     s0, s1, ref, ref64, p = _clump(xp, sc, oracle, 0, 150, 1, lanes)
-    compare(s1, ref, ref64, perturbed=perturbed_runs(oracle, sc, s0, xp=xp))
+    compare(s1, ref, ref64, perturbed=perturbed_runs(oracle, sc, s0, xp=xp, count=6, positions=True))
 
 
 def test_crowded_clump_water(xp, oracle, built_lib):
     sc = xp.scenes.config_dam_breach(scale=0.05)
     s0, s1, ref, ref64, p = _clump(xp, sc, oracle, 5, 150, 6)
-    compare(s1, ref, ref64, has_pbf=True, perturbed=perturbed_runs(oracle, sc, s0, xp=xp))
+    compare(s1, ref, ref64, has_pbf=True,
+            perturbed=perturbed_runs(oracle, sc, s0, xp=xp, count=6, positions=True))
 
 
 def test_batch_with_an_empty_scene(xp, oracle, built_lib):

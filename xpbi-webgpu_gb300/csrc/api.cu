@@ -280,6 +280,7 @@ struct xpbi_sim {
   uint32_t* matWords = nullptr;  // packed reference material table [S*128] (renderer binding)
   bool dirty = true;
   bool fresh = true;
+  bool waterLPending = false;  // a substep ran since the water particles' L was last formed
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   std::string gkey;
@@ -812,6 +813,7 @@ int xpbi_encode_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water) {
   enqueueSubstep(sim, schedule(sim), sim->stream, nullptr);
   XPBI_CK(cudaGetLastError());
   sim->fresh = false;
+  sim->waterLPending = true;
   return XPBI_OK;
 }
 
@@ -826,6 +828,7 @@ int xpbi_step(xpbi_sim* sim, int32_t substeps, int32_t iterations, int32_t has_w
   XPBI_TRY(ensureGraph(sim, schedule(sim)));
   for (int i = 0; i < substeps; ++i) XPBI_CK(cudaGraphLaunch(sim->gexec, sim->stream));
   sim->fresh = false;
+  sim->waterLPending = true;
   return XPBI_OK;
 }
 
@@ -846,6 +849,11 @@ int xpbi_read_state(xpbi_sim* sim, uint32_t scene, float* pos4, float* vel4, flo
                     uint32_t* sorted_idx, uint32_t* cell_tab) {
   XPBI_TRY(checkSim(sim));
   if (scene >= sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
+  if (L12 && sim->waterLPending && sim->b.N > 0) {
+    launch_computeL_water(sim->b, sim->stream);
+    XPBI_CK(cudaGetLastError());
+    sim->waterLPending = false;
+  }
   XPBI_TRY(xpbi_synchronize(sim));
   const SceneHost& h = sim->sc[scene];
   const Bufs& b = sim->b;
@@ -999,6 +1007,7 @@ int xpbi_profile_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water, f
   XPBI_CK(cudaGetLastError());
   XPBI_CK(cudaStreamSynchronize(sim->stream));
   sim->fresh = false;
+  sim->waterLPending = true;
   std::string text;
   const int nl = (int)lab.size();
   for (int k = 0; k < nl; ++k) {

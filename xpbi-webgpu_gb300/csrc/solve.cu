@@ -270,6 +270,29 @@ __device__ __forceinline__ uint32_t recordCandidates(const SceneDev& S, const ui
 }
 
 // ---------------------------------------------------------------- computeL
+// L of slot i (simkernels.js:198-220) over its recorded neighbours: the
+// SVD pseudo-inverse of sum V_b (grad W_b) (x_b - x_i)^T.
+__device__ __forceinline__ void bonetLok(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi) {
+  const SceneDev& S = *cx.scene;
+  const float4* __restrict__ posS = b.posS;
+  const float4* __restrict__ velIn = b.velS[0];  // only V^n (.w) is read, which no pass changes
+  M3 A = mzero();
+  forNbrs(b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
+          [&](uint32_t, bool, const PV& d) {
+            const V3 pb = xyz(d.p);
+            const V3 g = gradWFast(S, xi - pb);
+            const V3 r = pb - xi;
+            const M3 o = {{g * r.x, g * r.y, g * r.z}};
+            A = madd(A, mscale(o, d.v.w));
+          });
+  const SVD s = svd3Fast(A);
+  const float tol = 0.2f;
+  V3 inv = splat(0.f);
+  if (fabsf(s.sig.x) > tol) inv.x = __frcp_rn(s.sig.x);
+  if (fabsf(s.sig.y) > tol) inv.y = __frcp_rn(s.sig.y);
+  if (fabsf(s.sig.z) > tol) inv.z = __frcp_rn(s.sig.z);
+  storeM(b.L, b.N, i, diagMul(s.V, inv, s.U));
+}
 // Bonet-Lok correction with SVD pseudo-inverse (simkernels.js:189-221); its
 // candidate walk records the substep's neighbour list.
 __global__ void XPBI_LB_COMPUTEL k_computeL(Bufs b) {
@@ -288,22 +311,20 @@ __global__ void XPBI_LB_COMPUTEL k_computeL(Bufs b) {
     return dot(d, d) < s2;
   });
   b.nbrCount[i] = cnt <= kNbrCap ? cnt : kNbrOverflow;
-  M3 A = mzero();
-  forNbrs(b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
-          [&](uint32_t, bool, const PV& d) {
-            const V3 pb = xyz(d.p);
-            const V3 g = gradWFast(S, xi - pb);
-            const V3 r = pb - xi;
-            const M3 o = {{g * r.x, g * r.y, g * r.z}};
-            A = madd(A, mscale(o, d.v.w));
-          });
-  const SVD s = svd3Fast(A);
-  const float tol = 0.2f;
-  V3 inv = splat(0.f);
-  if (fabsf(s.sig.x) > tol) inv.x = __frcp_rn(s.sig.x);
-  if (fabsf(s.sig.y) > tol) inv.y = __frcp_rn(s.sig.y);
-  if (fabsf(s.sig.z) > tol) inv.z = __frcp_rn(s.sig.z);
-  storeM(b.L, b.N, i, diagMul(s.V, inv, s.U));
+  // no pass of the substep reads a water particle's correction (every
+  // velocity gradient is a solid's): k_computeL_water forms it when the state
+  // is read
+  if (!waterW(posS[i].w)) bonetLok(b, cx, i, xi);
+}
+
+// The water particles' L of the last substep, from the same positions,
+// neighbour lists and V^n as k_computeL would have used.
+__global__ void XPBI_LB_COMPUTEL k_computeL_water(Bufs b) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.N) return;
+  const float4 pi = b.posS[i];
+  if (!waterW(pi.w)) return;
+  bonetLok(b, ctxOf(b, i), i, xyz(pi));
 }
 
 // The record solveB gathers from each solid neighbour, in four float4
@@ -1170,6 +1191,7 @@ inline unsigned gridOf(uint32_t n, int block) { return (unsigned)((n + (uint32_t
 }  // namespace
 
 void launch_computeL(const Bufs& b, cudaStream_t st) { k_computeL<<<grid(b.N), kThreads, 0, st>>>(b); }
+void launch_computeL_water(const Bufs& b, cudaStream_t st) { k_computeL_water<<<grid(b.N), kThreads, 0, st>>>(b); }
 template <int V>
 void solveAVariant(const Bufs& b, int k, const float4* velIn, int flags, cudaStream_t st) {
   if (flags & kTrackResid)
