@@ -568,6 +568,7 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   A(b.FS, 9 * n);
   A(b.stateS, n);
   A(b.L, 9 * n);
+  A(b.sgP, 3 * n);
   A(b.lam, n);
   A(b.pbfLam, n);
   A(b.Sp, 4 * n);

@@ -271,20 +271,47 @@ __device__ __forceinline__ uint32_t recordCandidates(const SceneDev& S, const ui
 
 // ---------------------------------------------------------------- computeL
 // L of slot i (simkernels.js:198-220) over its recorded neighbours: the
-// SVD pseudo-inverse of sum V_b (grad W_b) (x_b - x_i)^T.
+// SVD pseudo-inverse of sum V_b (grad W_b) (x_b - x_i)^T. For a solid
+// (kSolid) the same sweep also forms the sums of the constraint passes that
+// no velocity enters — s = sum V_b g_b, P = sum (V_b^2 / m_b) g_b g_b^T and
+// the solid neighbour count, over the solid neighbours in list order — and
+// stores them in sgP for every iteration of the substep.
+template <bool kSolid>
 __device__ __forceinline__ void bonetLok(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi) {
   const SceneDev& S = *cx.scene;
   const float4* __restrict__ posS = b.posS;
   const float4* __restrict__ velIn = b.velS[0];  // only V^n (.w) is read, which no pass changes
   M3 A = mzero();
+  V3 sg = splat(0.f);
+  float p00 = 0.f, p11 = 0.f, p22 = 0.f, p01 = 0.f, p02 = 0.f, p12 = 0.f, cnt = 0.f;
   forNbrs(b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
-          [&](uint32_t, bool, const PV& d) {
+          [&](uint32_t, bool water, const PV& d) {
             const V3 pb = xyz(d.p);
             const V3 g = gradWFast(S, xi - pb);
             const V3 r = pb - xi;
             const M3 o = {{g * r.x, g * r.y, g * r.z}};
             A = madd(A, mscale(o, d.v.w));
+            if (kSolid && !water) {
+              const float Vb = d.v.w;
+              sg = sg + g * Vb;
+              const float c = Vb * Vb / cx.mats[matOfW(d.p.w)].mass;
+              const V3 cg = g * c;
+              p00 += cg.x * g.x;
+              p11 += cg.y * g.y;
+              p22 += cg.z * g.z;
+              p01 += cg.x * g.y;
+              p02 += cg.x * g.z;
+              p12 += cg.y * g.z;
+              cnt += 1.f;
+            }
           });
+  if constexpr (kSolid) {
+    float4* __restrict__ R = b.sgP + i;
+    const size_t N = b.N;
+    R[0] = make_float4(sg.x, sg.y, sg.z, cnt);
+    R[N] = make_float4(p00, p11, p22, p01);
+    R[2 * N] = make_float4(p02, p12, 0.f, 0.f);
+  }
   const SVD s = svd3Fast(A);
   const float tol = 0.2f;
   V3 inv = splat(0.f);
@@ -314,7 +341,7 @@ __global__ void XPBI_LB_COMPUTEL k_computeL(Bufs b) {
   // no pass of the substep reads a water particle's correction (every
   // velocity gradient is a solid's): k_computeL_water forms it when the state
   // is read
-  if (!waterW(posS[i].w)) bonetLok(b, cx, i, xi);
+  if (!waterW(posS[i].w)) bonetLok<true>(b, cx, i, xi);
 }
 
 // The water particles' L of the last substep, from the same positions,
@@ -324,7 +351,7 @@ __global__ void XPBI_LB_COMPUTEL k_computeL_water(Bufs b) {
   if (i >= b.N) return;
   const float4 pi = b.posS[i];
   if (!waterW(pi.w)) return;
-  bonetLok(b, ctxOf(b, i), i, xyz(pi));
+  bonetLok<false>(b, ctxOf(b, i), i, xyz(pi));
 }
 
 // The record solveB gathers from each solid neighbour, in four float4
@@ -409,26 +436,51 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
   M3 A = mzero();
   V3 sg = splat(0.f);
   float p00 = 0.f, p11 = 0.f, p22 = 0.f, p01 = 0.f, p02 = 0.f, p12 = 0.f, cnt = 0.f;
-  forNbrsLanes<NL>(
-      b, cx, i, xi, lane, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
-          [&](uint32_t, bool water, const PV& d) {
-            if (water) return;
-            const V3 g = gradWFast(S, xi - xyz(d.p));
-            const float Vb = d.v.w;
-            const V3 dv = (xyz(d.v) - vi) * Vb;
-            A = madd(A, M3{{dv * g.x, dv * g.y, dv * g.z}});
-            sg = sg + g * Vb;
-            const float c = Vb * Vb / cx.mats[matOfW(d.p.w)].mass;
-            const V3 cg = g * c;
-            p00 += cg.x * g.x;
-            p11 += cg.y * g.y;
-            p22 += cg.z * g.z;
-            p01 += cg.x * g.y;
-            p02 += cg.x * g.z;
-            p12 += cg.y * g.z;
-            cnt += 1.f;
-          },
-      SolidOnly{});
+  if constexpr (NL == 1) {
+    // s, P and the count do not depend on the velocities: computeL formed
+    // them in the same order, so the sweep only accumulates A
+    forNbrs(
+        b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
+        [&](uint32_t, bool water, const PV& d) {
+          if (water) return;
+          const V3 g = gradWFast(S, xi - xyz(d.p));
+          const V3 dv = (xyz(d.v) - vi) * d.v.w;
+          A = madd(A, M3{{dv * g.x, dv * g.y, dv * g.z}});
+        },
+        SolidOnly{});
+    const float4* __restrict__ R = b.sgP + i;
+    const size_t N = b.N;
+    const float4 r0 = R[0], r1 = R[N], r2 = R[2 * N];
+    sg = xyz(r0);
+    cnt = r0.w;
+    p00 = r1.x;
+    p11 = r1.y;
+    p22 = r1.z;
+    p01 = r1.w;
+    p02 = r2.x;
+    p12 = r2.y;
+  } else {
+    forNbrsLanes<NL>(
+        b, cx, i, xi, lane, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
+        [&](uint32_t, bool water, const PV& d) {
+          if (water) return;
+          const V3 g = gradWFast(S, xi - xyz(d.p));
+          const float Vb = d.v.w;
+          const V3 dv = (xyz(d.v) - vi) * Vb;
+          A = madd(A, M3{{dv * g.x, dv * g.y, dv * g.z}});
+          sg = sg + g * Vb;
+          const float c = Vb * Vb / cx.mats[matOfW(d.p.w)].mass;
+          const V3 cg = g * c;
+          p00 += cg.x * g.x;
+          p11 += cg.y * g.y;
+          p22 += cg.z * g.z;
+          p01 += cg.x * g.y;
+          p02 += cg.x * g.z;
+          p12 += cg.y * g.z;
+          cnt += 1.f;
+        },
+        SolidOnly{});
+  }
   if constexpr (NL > 1) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) A.c[c] = laneSum<NL>(A.c[c]);

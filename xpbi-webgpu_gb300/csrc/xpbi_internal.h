@@ -98,6 +98,8 @@ struct Bufs {
   float* FS;            // [9][N] sorted F
   float* stateS;        // [N] sorted plastic state
   float* L;             // [9][N] kernel-gradient correction
+  float4* sgP;          // [3][N] a solid's velocity-free sums over its solid neighbours (computeL):
+                        //   (sum V g, count), (P00, P11, P22, P01), (P02, P12, -, -), P = sum V^2/m g g^T
   float* lam;           // [N] XPBI multiplier
   float* pbfLam;        // [N] PBF multiplier
   float4* Sp;           // [4][N] solveB neighbour record planes: dlam G L columns (x, y, z in .w), x + dt v, mass
