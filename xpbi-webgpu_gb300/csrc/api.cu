@@ -434,7 +434,9 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
   R.mark(st, "fill");
   launch_reorder(b, sch.keepLam, st);
   R.mark(st, "reorder");
-  launch_computeL(b, st);
+  // the velocity-free sums are read by the one-lane constraint sweeps (and
+  // the features pass, which always has one lane)
+  launch_computeL(b, sch.lanes == 1 || sch.features, st);
   R.mark(st, "computeL");
   if (sch.features) {
     launch_features(b, b.velS[0], st);
@@ -454,9 +456,8 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
     cudaMemsetAsync(b.itersUsed, 0, sizeof(int) * b.S, st);
   }
   const int aflags = (sch.reduce ? kTrackResid : 0) | (sch.mode != 0 ? kWarm : 0);
-  // solveA(k) records the scenes' largest solid displacement in slot k & 1,
-  // solveB(k) clears the other slot for the next iteration
-  cudaMemsetAsync(b.solidDisp, 0, sizeof(uint32_t) * 2 * b.S, st);
+  // solveA(k) records the scenes' largest solid displacement in slot k & 1
+  // (the reorder cleared both), solveB(k) clears the other for iteration k+1
   int in = 0;
   for (int k = 0; k < sch.K; ++k) {
     // iteration 0 after a features pass: that pass already evaluated the
@@ -1081,7 +1082,7 @@ int xpbi_autotune(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t 
     launch_scan(b, st);
     launch_scatter(b, st);
     launch_reorder(b, false, st);
-    launch_computeL(b, st);
+    launch_computeL(b, true, st);
     cudaMemsetAsync(b.done, 0, sizeof(int) * b.S, st);  // no scene counts as converged here
     cudaMemsetAsync(b.solidDisp, 0, sizeof(uint32_t) * 2 * b.S, st);
     // iteration 0 of each variant from lambda = 0, then solveB on its record

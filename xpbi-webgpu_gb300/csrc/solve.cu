@@ -289,8 +289,15 @@ __device__ __forceinline__ void bonetLok(const Bufs& b, const Ctx& cx, uint32_t 
             const V3 pb = xyz(d.p);
             const V3 g = gradWFast(S, xi - pb);
             const V3 r = pb - xi;
-            const M3 o = {{g * r.x, g * r.y, g * r.z}};
-            A = madd(A, mscale(o, d.v.w));
+            // A += V_b g r^T with every rounding explicit, so the two
+            // instances (with and without the sums below) form the same L
+            const float Vb0 = d.v.w;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              A.c[c].x = __fmaf_rn(__fmul_rn(g.x, r[c]), Vb0, A.c[c].x);
+              A.c[c].y = __fmaf_rn(__fmul_rn(g.y, r[c]), Vb0, A.c[c].y);
+              A.c[c].z = __fmaf_rn(__fmul_rn(g.z, r[c]), Vb0, A.c[c].z);
+            }
             if (kSolid && !water) {
               const float Vb = d.v.w;
               sg = sg + g * Vb;
@@ -322,6 +329,7 @@ __device__ __forceinline__ void bonetLok(const Bufs& b, const Ctx& cx, uint32_t 
 }
 // Bonet-Lok correction with SVD pseudo-inverse (simkernels.js:189-221); its
 // candidate walk records the substep's neighbour list.
+template <bool kSums>
 __global__ void XPBI_LB_COMPUTEL k_computeL(Bufs b) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
@@ -341,7 +349,7 @@ __global__ void XPBI_LB_COMPUTEL k_computeL(Bufs b) {
   // no pass of the substep reads a water particle's correction (every
   // velocity gradient is a solid's): k_computeL_water forms it when the state
   // is read
-  if (!waterW(posS[i].w)) bonetLok<true>(b, cx, i, xi);
+  if (!waterW(posS[i].w)) bonetLok<kSums>(b, cx, i, xi);
 }
 
 // The water particles' L of the last substep, from the same positions,
@@ -1242,7 +1250,12 @@ inline unsigned gridOf(uint32_t n, int block) { return (unsigned)((n + (uint32_t
 
 }  // namespace
 
-void launch_computeL(const Bufs& b, cudaStream_t st) { k_computeL<<<grid(b.N), kThreads, 0, st>>>(b); }
+void launch_computeL(const Bufs& b, bool sums, cudaStream_t st) {
+  if (sums)
+    k_computeL<true><<<grid(b.N), kThreads, 0, st>>>(b);
+  else
+    k_computeL<false><<<grid(b.N), kThreads, 0, st>>>(b);
+}
 void launch_computeL_water(const Bufs& b, cudaStream_t st) { k_computeL_water<<<grid(b.N), kThreads, 0, st>>>(b); }
 template <int V>
 void solveAVariant(const Bufs& b, int k, const float4* velIn, int flags, cudaStream_t st) {

@@ -156,7 +156,8 @@ void launch_warm_from_prev(const Bufs& b, cudaStream_t st);
 uint32_t scan_tiles(uint32_t cells);
 
 // ---- launchers (solve.cu) ----
-void launch_computeL(const Bufs& b, cudaStream_t st);
+// sums: also form the solids' velocity-free constraint sums (sgP)
+void launch_computeL(const Bufs& b, bool sums, cudaStream_t st);
 // the water particles' L of the last substep (computeL forms the solids' only)
 void launch_computeL_water(const Bufs& b, cudaStream_t st);
 void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, int variant, int lanes, cudaStream_t st);
