@@ -319,7 +319,9 @@ def run_xpbi(args, rank: int, world: int):
 
     # ---- end to end through the public API with host buffers: per step the
     # frame's writeParams from host memory, one substep, and the positions
-    # read back into pinned host memory
+    # read back into pinned host memory (asynchronously, like the
+    # reference's mapAsync: a step's read-back overlaps the next substep;
+    # all are complete when the final synchronize returns)
     pinned = [torch.empty((len(s["positions"]), 4), dtype=torch.float32, pin_memory=True).numpy()
               for s in scenes]
     params = [xp.params_for(s) for s in scenes]
@@ -332,7 +334,8 @@ def run_xpbi(args, rank: int, world: int):
             sim.write_params(params[k], scene=k)
         sim.step(1, -1, has_water)
         for k in range(len(scenes)):
-            sim.read_pos(k, out=pinned[k])
+            sim.read_pos_async(k, pinned[k])
+    sim.synchronize()
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
     e2e = job_throughput(n_total, world, args.steps, e2e_s)

@@ -150,6 +150,15 @@ int xpbi_set_stream(xpbi_sim* sim, void* cuda_stream);
 /* __XPBI.readPos / readVel (main.js:291-312): vec4 x N of scene `scene`
  * (0 for single-scene handles), in the current (cell-sorted) order. */
 int xpbi_read_positions(xpbi_sim* sim, uint32_t scene, float* out_pos4);
+
+/* Asynchronous form of xpbi_read_positions, like the reference's mapAsync
+ * read-back (main.js:291-312): enqueues the copy of the scene's current
+ * positions into out_pos4 behind the work enqueued so far and returns at
+ * once. out_pos4 should be page-locked host memory, and it holds the
+ * positions once xpbi_synchronize returns. Later substeps wait for the copy
+ * before they move the particles, so read-back overlaps the next substep.
+ * No counterpart in the reference's C surface. */
+int xpbi_read_positions_async(xpbi_sim* sim, uint32_t scene, float* out_pos4);
 int xpbi_read_velocities(xpbi_sim* sim, uint32_t scene, float* out_vel4);
 
 /* Full state of one scene in the reference layouts; any pointer may be NULL.

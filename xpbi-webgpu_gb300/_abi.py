@@ -30,7 +30,7 @@ EXPORTS = (
     "xpbi_mlp_param_count", "xpbi_mlp_forward", "xpbi_mlp_grad", "xpbi_mlp_train",
     "xpbi_set_solver", "xpbi_set_network", "xpbi_read_residuals", "xpbi_read_training",
     "xpbi_sort_cells_noalloc", "xpbi_read_contact_residuals", "xpbi_autotune", "xpbi_set_variants",
-    "xpbi_render", "xpbi_set_lanes",
+    "xpbi_render", "xpbi_set_lanes", "xpbi_read_positions_async",
 )
 
 
@@ -110,6 +110,7 @@ _SIGS = {
     "xpbi_autotune": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32), _F32P, C.c_int32]),
     "xpbi_set_variants": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "xpbi_set_lanes": (C.c_int, [_P, C.c_int32]),
+    "xpbi_read_positions_async": (C.c_int, [_P, C.c_uint32, _F32P]),
     "xpbi_render": (C.c_int, [_P, C.c_uint32, C.POINTER(Camera), C.c_uint32, C.c_uint32, C.POINTER(C.c_uint8),
                               C.POINTER(_P)]),
     "xpbi_sort_cells_noalloc": (C.c_int, [_P, C.c_uint32, _F32P, C.c_float, C.POINTER(C.c_int32), _P, _P, _P]),

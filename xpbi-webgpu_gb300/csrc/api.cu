@@ -281,6 +281,12 @@ struct xpbi_sim {
   bool dirty = true;
   bool fresh = true;
   bool waterLPending = false;  // a substep ran since the water particles' L was last formed
+  // asynchronous position read-back (xpbi_read_positions_async): a copy
+  // stream that waits for the work enqueued so far; a substep's position
+  // update waits for the copies (an external event wait, also in graphs)
+  cudaStream_t copy = nullptr;
+  cudaEvent_t evWork = nullptr, evCopy = nullptr;
+  bool copyPending = false;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   std::string gkey;
@@ -330,6 +336,17 @@ void destroyAll(xpbi_sim* s) {
   if (s->renderRgba) cudaFree(s->renderRgba);
   if (s->own) cudaStreamDestroy(s->own);
   if (s->capture) cudaStreamDestroy(s->capture);
+  if (s->copy) cudaStreamDestroy(s->copy);
+  if (s->evWork) cudaEventDestroy(s->evWork);
+  if (s->evCopy) cudaEventDestroy(s->evCopy);
+}
+
+// Work outside the substep that rewrites the positions waits for the
+// asynchronous read-backs enqueued before it.
+void drainCopies(xpbi_sim* s) {
+  if (!s->copyPending) return;
+  cudaStreamWaitEvent(s->stream, s->evCopy, 0);
+  s->copyPending = false;
 }
 
 int upload(xpbi_sim* s) {
@@ -493,6 +510,14 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
   launch_xsph(b, b.velS[in], b.velS[in ^ 1], st);
   R.mark(st, "xsph");
   in ^= 1;
+  // the update moves the particles: asynchronous read-backs of the previous
+  // positions (xpbi_read_positions_async) must have finished (inside a
+  // captured graph, as an external event wait node)
+  {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(st, &cs);
+    cudaStreamWaitEvent(st, s->evCopy, cs == cudaStreamCaptureStatusActive ? cudaEventWaitExternal : 0);
+  }
   launch_updateF_integrate(b, b.velS[in], st);
   R.mark(st, "updateF+integrate");
   if (sch.keepLam) {
@@ -545,7 +570,10 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   };
   if (cudaGetDevice(&s->device) != cudaSuccess) return bail(fail(XPBI_ERR_CUDA, "no CUDA device"));
   if (cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&s->capture, cudaStreamNonBlocking) != cudaSuccess)
+      cudaStreamCreateWithFlags(&s->capture, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&s->evWork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&s->evCopy, cudaEventDisableTiming) != cudaSuccess)
     return bail(fail(XPBI_ERR_CUDA, "cudaStreamCreate failed"));
   s->stream = s->own;
   Bufs& b = s->b;
@@ -759,6 +787,7 @@ int xpbi_batch_create(const xpbi_scene_desc* scenes, uint32_t n_scenes, xpbi_sim
 void xpbi_destroy(xpbi_sim* sim) {
   if (!sim) return;
   cudaStreamSynchronize(sim->stream);
+  if (sim->copy) cudaStreamSynchronize(sim->copy);
   destroyAll(sim);
   delete sim;
 }
@@ -837,12 +866,14 @@ int xpbi_step(xpbi_sim* sim, int32_t substeps, int32_t iterations, int32_t has_w
 int xpbi_synchronize(xpbi_sim* sim) {
   XPBI_TRY(checkSim(sim));
   XPBI_CK(cudaStreamSynchronize(sim->stream));
+  if (sim->copy) XPBI_CK(cudaStreamSynchronize(sim->copy));
+  sim->copyPending = false;
   return checkDeviceErr(sim);
 }
 
 int xpbi_set_stream(xpbi_sim* sim, void* cuda_stream) {
   XPBI_TRY(checkSim(sim));
-  XPBI_CK(cudaStreamSynchronize(sim->stream));
+  XPBI_TRY(xpbi_synchronize(sim));
   sim->stream = cuda_stream ? (cudaStream_t)cuda_stream : sim->own;
   return XPBI_OK;
 }
@@ -915,6 +946,20 @@ int xpbi_read_positions(xpbi_sim* sim, uint32_t scene, float* out_pos4) {
   return xpbi_synchronize(sim);
 }
 
+int xpbi_read_positions_async(xpbi_sim* sim, uint32_t scene, float* out_pos4) {
+  XPBI_TRY(checkSim(sim));
+  if (!out_pos4) return fail(XPBI_ERR_INVALID, "output is NULL");
+  if (scene >= sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
+  const SceneHost& h = sim->sc[scene];
+  if (h.n == 0) return XPBI_OK;
+  XPBI_CK(cudaEventRecord(sim->evWork, sim->stream));
+  XPBI_CK(cudaStreamWaitEvent(sim->copy, sim->evWork, 0));
+  XPBI_CK(cudaMemcpyAsync(out_pos4, sim->b.pos + h.pBase, 16 * (size_t)h.n, cudaMemcpyDeviceToHost, sim->copy));
+  XPBI_CK(cudaEventRecord(sim->evCopy, sim->copy));
+  sim->copyPending = true;
+  return XPBI_OK;
+}
+
 int xpbi_read_velocities(xpbi_sim* sim, uint32_t scene, float* out_vel4) {
   XPBI_TRY(checkSim(sim));
   if (!out_vel4) return fail(XPBI_ERR_INVALID, "output is NULL");
@@ -928,6 +973,7 @@ int xpbi_read_velocities(xpbi_sim* sim, uint32_t scene, float* out_vel4) {
 int xpbi_write_state(xpbi_sim* sim, uint32_t scene, const float* pos4, const float* vel4, const float* F12,
                      const float* aux4) {
   XPBI_TRY(checkSim(sim));
+  XPBI_TRY(xpbi_synchronize(sim));  // read-backs in flight finish first
   if (scene >= sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
   XPBI_CK(cudaStreamSynchronize(sim->stream));
   const SceneHost& h = sim->sc[scene];
@@ -992,6 +1038,7 @@ int xpbi_info(xpbi_sim* sim, uint32_t* n_particles, uint32_t* n_cells, uint32_t*
 int xpbi_profile_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water, float* ms, int32_t cap,
                          int32_t* count, char* labels, size_t labels_cap) {
   XPBI_TRY(checkSim(sim));
+  drainCopies(sim);
   for (const SceneHost& h : sim->sc)
     if (!(h.params.dt > 0.f)) return fail(XPBI_ERR_INVALID, "write_params must be called before stepping");
   XPBI_TRY(applySchedule(sim, iterations, has_water));
@@ -1033,6 +1080,7 @@ int xpbi_profile_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water, f
 int xpbi_autotune(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t repeats, int32_t* chosen,
                   float* ms, int32_t cap) {
   XPBI_TRY(checkSim(sim));
+  drainCopies(sim);
   for (const SceneHost& h : sim->sc)
     if (!(h.params.dt > 0.f)) return fail(XPBI_ERR_INVALID, "write_params must be called before xpbi_autotune");
   if (repeats < 1 || repeats > 1000) return fail(XPBI_ERR_INVALID, "repeats must be 1..1000");

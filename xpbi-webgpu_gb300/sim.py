@@ -205,6 +205,16 @@ class Simulation:
         check(lib().xpbi_read_positions(self._h, scene, _fptr(a)))
         return a
 
+    def read_pos_async(self, scene: int, out):
+        """Enqueue the read-back of the scene's positions into `out` (an
+        (n, 4) float32 array, ideally in page-locked memory); the values are
+        there once synchronize() returns. Keep `out` alive until then."""
+        n = self.scene_sizes[scene]
+        if out.shape != (n, 4) or out.dtype != np.float32 or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a C-contiguous (n, 4) float32 array")
+        check(lib().xpbi_read_positions_async(self._h, scene, _fptr(out)))
+        return out
+
     def read_vel(self, scene: int = 0, out=None):
         n = self.scene_sizes[scene]
         a = out if out is not None else np.empty((n, 4), np.float32)
