@@ -53,7 +53,7 @@ ALGO_BYTES = {"solveA": (196, 16), "solveB": (128, 48), "pbfA": (36, 36), "pbfB"
 # dram__bytes_write.sum over particles) from an ncu --set full capture of the
 # current kernels on the 1M-particle dam breach; the traffic of a launch grows
 # with the particle count, so the bench scales it by the workload's.
-NCU_TRAFFIC_PER_PARTICLE = {"solveB": 127.0, "solveA": 136.8, "pbfA": 105.5, "computeL": 229.5}
+NCU_TRAFFIC_PER_PARTICLE = {"solveB": 127.8, "solveA": 153.7, "pbfA": 105.6, "computeL": 229.5}
 
 
 def workload(name: str, rank: int = 0):
