@@ -888,7 +888,8 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveB(Bufs b, int k, const f
                                                       float4* __restrict__ velOut, int writeXc, int flags) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t i = t / G, lane = t % G;
-  if (t < b.S) b.solidDisp[(size_t)((k + 1) & 1) * b.S + t] = 0u;  // the next iteration's slot
+  for (uint32_t q = t; q < b.S; q += gridDim.x * blockDim.x)  // the next iteration's slot
+    b.solidDisp[(size_t)((k + 1) & 1) * b.S + q] = 0u;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;

@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(kBigThreads) k_bigcells(Bufs b, uint32_t* scra
 __global__ void __launch_bounds__(kThreads) k_reorder(Bufs b, int keepLam) {
   uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   // both slots of the substep's largest-solid-displacement ring start at 0
-  if (p < 2u * b.S) b.solidDisp[p] = 0u;
+  for (uint32_t q = p; q < 2u * b.S; q += gridDim.x * blockDim.x) b.solidDisp[q] = 0u;
   if (p >= b.N) return;
   uint32_t i = b.tmp[p];
   uint32_t key = b.key[i];
