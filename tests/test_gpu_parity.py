@@ -80,6 +80,31 @@ def test_dam_breach_fast_water(xp, oracle, built_lib):
     compare(s1, ref, ref64, has_pbf=True)
 
 
+def test_fast_solids_contact_reach(xp, oracle, built_lib):
+    """Sand thrown in random directions at up to 4 m/s while it presses on
+    the floor: solveB loads a neighbour's predicted position only within
+    minD + dt |v_i| + the scene's largest solid displacement, so large and
+    uneven displacements must still find every contact pair."""
+    sc = xp.scenes.config_sand_column()
+    p = xp.params_for(sc)
+    it = sc["iterations"]
+    with xp.Simulation(sc) as sim:
+        sim.write_params(p)
+        sim.step(200, it, False)
+        st = sim.read_state()
+        rng = np.random.default_rng(5)
+        vel = st["vel"].copy()
+        vel[:, :3] += rng.uniform(-4.0, 4.0, size=(len(vel), 3)).astype(np.float32)
+        sim.write_state(0, vel=vel)
+        s0 = sim.read_state()
+        pw, mw = sim.uniforms()
+        ref = oracle.substep(pw, mw, s0, it, False, -1)
+        ref64 = oracle.substep(pw, mw, s0, it, False, -1, f64=True)
+        sim.encode_substep(it, False)
+        s1 = sim.read_state()
+    compare(s1, ref, ref64, perturbed=perturbed_runs(oracle, sc, s0, xp=xp))
+
+
 def test_reference_pbf_interleave(xp, oracle, built_lib):
     """pbfIterations unset: one PBF pass after every XPBI iteration."""
     sc = xp.scenes.config_dam_breach(scale=0.05)
