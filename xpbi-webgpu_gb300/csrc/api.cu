@@ -528,11 +528,11 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
 
 int kernelsPerSubstep(const Schedule& sch) {
   int n = 5 /* count, scan, fill, bigcells, reorder */ + 1 /* computeL */ + 2 /* xsph, updateF+integrate */;
-  for (int k = 0; k < sch.K; ++k) n += 2 + (sch.pbf[k] ? 2 : 0) + (sch.reduce ? 2 : 0);
+  for (int k = 0; k < sch.K; ++k) n += 2 + (sch.pbf[k] ? 2 : 0) + (sch.reduce ? 1 : 0);
   if (sch.features) n += 1;
   if (sch.mode == 1) n += 2;
   if (sch.mode == 2) n += 1;
-  if (sch.track) n += 4;
+  if (sch.track) n += 3;
   if (sch.keepLam) n += 1;
   return n;
 }
@@ -632,6 +632,7 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   A(b.rc, n);
   A(b.solidDisp, 2 * (size_t)nScenes);
   A(b.residPart, (size_t)nScenes * kResidChunks * 3);
+  A(b.residTicket, nScenes);
   A(b.resid, (size_t)nScenes * kMaxResid);
   A(b.residC, (size_t)nScenes * kMaxResid);
   A(b.c0, nScenes);
@@ -687,6 +688,7 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
             cudaMemset(b.resid, 0, sizeof(double) * nScenes * kMaxResid) == cudaSuccess &&
             cudaMemset(b.residC, 0, sizeof(double) * nScenes * kMaxResid) == cudaSuccess &&
             cudaMemset(b.cc0, 0, sizeof(double) * nScenes) == cudaSuccess &&
+            cudaMemset(b.residTicket, 0, sizeof(uint32_t) * nScenes) == cudaSuccess &&
             cudaMemset(s->netErr, 0, sizeof(int)) == cudaSuccess &&
             cudaMemset(b.cellStart, 0, 4 * ((size_t)b.C + 4)) == cudaSuccess;
   if (!ok) return bail(fail(XPBI_ERR_CUDA, "initial upload failed"));

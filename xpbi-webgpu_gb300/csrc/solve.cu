@@ -68,6 +68,14 @@ constexpr int kSolveBBlock[kSolveBVariants] = {128, 128, 128, 64, 256};
 #else
 #define XPBI_LB_UPDATE XPBI_LB_DEFAULT
 #endif
+// The features pass (the constraint sweep of solveA plus the stored
+// constraint and features) at 7 CTAs per SM (72 registers, ~100 bytes of
+// spills outside the neighbour loop): 0.48 ms per 4M-particle substep against
+// 0.60 ms with the allocator's 94 registers and 0.52 ms at 6 CTAs.
+#ifndef XPBI_MINB_FEATURES
+#define XPBI_MINB_FEATURES 7
+#endif
+#define XPBI_LB_FEATURES __launch_bounds__(kThreads, XPBI_MINB_FEATURES)
 
 struct Ctx {
   const SceneDev* __restrict__ scene;
@@ -686,7 +694,7 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveA(Bufs b, int k, const f
 //   7    solid neighbours / 32
 //   8-14 material kind one-hot
 //   15   log10(mu) - 4.5
-__global__ void __launch_bounds__(kThreads) k_features(Bufs b, const float4* __restrict__ velIn) {
+__global__ void XPBI_LB_FEATURES k_features(Bufs b, const float4* __restrict__ velIn) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
@@ -711,7 +719,8 @@ __global__ void __launch_bounds__(kThreads) k_features(Bufs b, const float4* __r
     f[6] = log10f(1.f + c.denom / aT);
     f[7] = c.nNbr * (1.f / 32.f);
     const uint32_t kind = cx.mats[mi].kind;
-    if (kind < 7u) f[8 + kind] = 1.f;
+#pragma unroll
+    for (uint32_t q = 0; q < 7u; ++q) f[8 + q] = kind == q ? 1.f : 0.f;  // constant indices: f stays in registers
     f[15] = log10f(fmaxf(m.mu, 1e-6f)) - 4.5f;
   }
   float4* out = reinterpret_cast<float4*>(b.feat + (size_t)i * kFeat);
@@ -736,50 +745,19 @@ __global__ void k_warm_from_prev(Bufs b) {
   b.lamWarm[i] = b.lamPrev[i];
 }
 
-// Per-scene residual norms, deterministic: block (c, s) sums chunk c of
-// scene s in a fixed order; k_resid_final adds the chunks in order.
+// Per-scene residual norms, deterministic, in one launch: warp w of block
+// (x, s) sums chunk 8x + w of scene s in a fixed order and stores the
+// chunk's partial sums; the last of the scene's blocks to finish (a ticket
+// counter, no waiting) adds the chunks in chunk order, so the totals do not
+// depend on which block comes last. One wave of blocks whose warps each
+// stream a chunk with float4 loads: the per-block chains of dependent loads,
+// barriers and fences are few.
 // Sums: constraint residual^2, (iteration 0) residual^2 at lambda = 0,
 // contact correction^2.
 // Chunk sums are formed in f32 (a convergence test on sums of squares needs
-// nothing finer, and f64 is slow here) by a fixed warp butterfly and a fixed
-// combine of the 8 warps; the chunks are added in f64.
-constexpr int kResidSums = 3;
-__global__ void __launch_bounds__(256) k_resid_partial(Bufs b, int k) {
-  __shared__ float red[kResidSums][8];
-  const uint32_t s = blockIdx.y, c = blockIdx.x;
-  const SceneDev& S = b.scenes[s];
-  const uint32_t n = S.n, base = S.pBase;
-  const uint32_t lo = base + (uint32_t)(((uint64_t)n * c) / kResidChunks);
-  const uint32_t hi = base + (uint32_t)(((uint64_t)n * (c + 1)) / kResidChunks);
-  float a = 0.f, a0 = 0.f, ac = 0.f;
-  if (!b.done[s] || k < 0) {
-    for (uint32_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
-      a += b.rr[p];
-      ac += b.rc[p];
-      if (k == 0) a0 += b.c0sq[p];
-    }
-  }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    a += __shfl_xor_sync(0xffffffffu, a, off);
-    a0 += __shfl_xor_sync(0xffffffffu, a0, off);
-    ac += __shfl_xor_sync(0xffffffffu, ac, off);
-  }
-  const uint32_t w = threadIdx.x >> 5;
-  if ((threadIdx.x & 31u) == 0) {
-    red[0][w] = a;
-    red[1][w] = a0;
-    red[2][w] = ac;
-  }
-  __syncthreads();
-  if (threadIdx.x < kResidSums) {
-    double t = 0.0;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) t += (double)red[threadIdx.x][q];
-    b.residPart[(s * kResidChunks + c) * kResidSums + threadIdx.x] = t;
-  }
-}
-
+// nothing finer, and f64 is slow here) in a fixed per-lane order and a fixed
+// warp butterfly; the chunks are added in f64.
+//
 // k >= 0: the residuals of the state entering iteration k (early stop),
 // reduced after iteration k's update; k < 0: after the last iteration (slot
 // kMaxResid - 1). A scene stops, skipping iterations k+1.., once both its
@@ -788,20 +766,46 @@ __global__ void __launch_bounds__(256) k_resid_partial(Bufs b, int k) {
 // which the constraint residual does not see). With a warm start, iteration
 // 0's constraint residual is the linearised estimate before the warm impulse
 // is applied, so it never stops the solve.
-// One warp per scene: lane l adds chunks l, l + 32, ... in order, then a
-// fixed butterfly combines the lanes, so the sums do not depend on timing.
-__global__ void k_resid_final(Bufs b, int k, int warm) {
-  const uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+constexpr int kResidSums = 3;
+constexpr int kResidWarps = 8;  // chunks per block, one warp each
+static_assert(kResidChunks % kResidWarps == 0, "whole blocks of chunks");
+__global__ void __launch_bounds__(32 * kResidWarps) k_resid(Bufs b, int k, int warm) {
+  __shared__ bool lastBlock;
+  const uint32_t s = blockIdx.y;
   const uint32_t lane = threadIdx.x & 31u;
-  if (s >= b.S) return;  // whole warps leave together
+  const uint32_t c = blockIdx.x * kResidWarps + (threadIdx.x >> 5);  // this warp's chunk
   const SceneDev& S = b.scenes[s];
-  if (k >= 0 && (b.done[s] || k >= S.iterations)) return;
-  double a = 0.0, a0 = 0.0, ac = 0.0;
-  for (int c = (int)lane; c < kResidChunks; c += 32) {
-    const double* part = b.residPart + (s * kResidChunks + c) * kResidSums;
-    a += part[0];
-    a0 += part[1];
-    ac += part[2];
+  const uint32_t n = S.n, base = S.pBase;
+  const uint32_t lo = base + (uint32_t)(((uint64_t)n * c) / kResidChunks);
+  const uint32_t hi = base + (uint32_t)(((uint64_t)n * (c + 1)) / kResidChunks);
+  float a = 0.f, a0 = 0.f, ac = 0.f;
+  if (!b.done[s] || k < 0) {
+    // the chunk's 16-byte-aligned interior as float4 (the arrays start on
+    // 256-byte boundaries), its ragged ends (< 4 slots each) as scalars
+    const uint32_t lo4 = min(hi, (lo + 3u) & ~3u), hi4 = max(lo4, hi & ~3u);
+    if (lo + lane < lo4) {
+      a += b.rr[lo + lane];
+      ac += b.rc[lo + lane];
+      if (k == 0) a0 += b.c0sq[lo + lane];
+    }
+    if (hi4 + lane < hi) {
+      a += b.rr[hi4 + lane];
+      ac += b.rc[hi4 + lane];
+      if (k == 0) a0 += b.c0sq[hi4 + lane];
+    }
+    const float4* __restrict__ rr4 = reinterpret_cast<const float4*>(b.rr);
+    const float4* __restrict__ rc4 = reinterpret_cast<const float4*>(b.rc);
+    const float4* __restrict__ c04 = reinterpret_cast<const float4*>(b.c0sq);
+#pragma unroll 4
+    for (uint32_t q = lo4 / 4u + lane; q < hi4 / 4u; q += 32u) {
+      const float4 x = rr4[q], y = rc4[q];
+      a += (x.x + x.y) + (x.z + x.w);
+      ac += (y.x + y.y) + (y.z + y.w);
+      if (k == 0) {
+        const float4 z = c04[q];
+        a0 += (z.x + z.y) + (z.z + z.w);
+      }
+    }
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
@@ -809,22 +813,55 @@ __global__ void k_resid_final(Bufs b, int k, int warm) {
     a0 += __shfl_xor_sync(0xffffffffu, a0, off);
     ac += __shfl_xor_sync(0xffffffffu, ac, off);
   }
+  if (lane == 0) {
+    double* part = b.residPart + (s * kResidChunks + c) * kResidSums;
+    part[0] = (double)a;
+    part[1] = (double)a0;
+    part[2] = (double)ac;
+    __threadfence();  // the partials are visible before this block's ticket
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();  // orders the warps' partials (published at the barrier) before the ticket
+    lastBlock = atomicAdd(b.residTicket + s, 1u) == gridDim.x - 1u;
+  }
+  __syncthreads();
+  if (!lastBlock || threadIdx.x >= 32u) return;
+  // the scene's last block, one warp: lane l adds chunks l, l + 32, ... in
+  // order (loads through L2: the other blocks' partials are not in this
+  // SM's L1), then a fixed butterfly combines the lanes
+  __threadfence();
+  if (lane == 0) b.residTicket[s] = 0u;  // every block of this launch has taken its ticket
+  if (k >= 0 && (b.done[s] || k >= S.iterations)) return;
+  double ta = 0.0, ta0 = 0.0, tac = 0.0;
+  for (int q = (int)lane; q < kResidChunks; q += 32) {
+    const double* part = b.residPart + (s * kResidChunks + q) * kResidSums;
+    ta += __ldcg(part);
+    ta0 += __ldcg(part + 1);
+    tac += __ldcg(part + 2);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    ta += __shfl_xor_sync(0xffffffffu, ta, off);
+    ta0 += __shfl_xor_sync(0xffffffffu, ta0, off);
+    tac += __shfl_xor_sync(0xffffffffu, tac, off);
+  }
   if (lane != 0) return;
   if (k < 0) {
-    b.resid[(size_t)s * kMaxResid + (kMaxResid - 1)] = a;
-    b.residC[(size_t)s * kMaxResid + (kMaxResid - 1)] = ac;
+    b.resid[(size_t)s * kMaxResid + (kMaxResid - 1)] = ta;
+    b.residC[(size_t)s * kMaxResid + (kMaxResid - 1)] = tac;
     return;
   }
   if (k < kMaxResid - 1) {
-    b.resid[(size_t)s * kMaxResid + k] = a;
-    b.residC[(size_t)s * kMaxResid + k] = ac;
+    b.resid[(size_t)s * kMaxResid + k] = ta;
+    b.residC[(size_t)s * kMaxResid + k] = tac;
   }
   if (k == 0) {
-    b.c0[s] = a0;
-    b.cc0[s] = ac;
+    b.c0[s] = ta0;
+    b.cc0[s] = tac;
   }
   const double tol = (double)S.residTol, tolC = (double)S.residTolC;
-  if (tol > 0.0 && a <= tol * tol * b.c0[s] && ac <= tolC * tolC * b.cc0[s] && !(warm && k == 0)) b.done[s] = 1;
+  if (tol > 0.0 && ta <= tol * tol * b.c0[s] && tac <= tolC * tolC * b.cc0[s] && !(warm && k == 0)) b.done[s] = 1;
   b.itersUsed[s] = k + 1;
 }
 
@@ -1299,8 +1336,7 @@ void launch_features(const Bufs& b, const float4* velIn, cudaStream_t st) {
 void launch_warm_from_net(const Bufs& b, cudaStream_t st) { k_warm_from_net<<<grid(b.N), kThreads, 0, st>>>(b); }
 void launch_warm_from_prev(const Bufs& b, cudaStream_t st) { k_warm_from_prev<<<grid(b.N), kThreads, 0, st>>>(b); }
 void launch_resid_reduce(const Bufs& b, int k, bool warm, cudaStream_t st) {
-  k_resid_partial<<<dim3(kResidChunks, b.S), 256, 0, st>>>(b, k);
-  k_resid_final<<<(b.S + 3) / 4, 128, 0, st>>>(b, k, warm ? 1 : 0);
+  k_resid<<<dim3(kResidChunks / kResidWarps, b.S), 32 * kResidWarps, 0, st>>>(b, k, warm ? 1 : 0);
 }
 void launch_keep_lambda(const Bufs& b, cudaStream_t st) { k_keep_lambda<<<grid(b.N), kThreads, 0, st>>>(b); }
 template <int V>

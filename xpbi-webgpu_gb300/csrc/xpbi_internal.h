@@ -133,6 +133,7 @@ struct Bufs {
   float* rc;            // [N] squared contact correction of the current iteration
   uint32_t* solidDisp;  // [2][S] float bits: largest dt |v| of a scene's solids entering iteration k (slot k & 1)
   double* residPart;    // [S][kResidChunks][3] partial sums
+  uint32_t* residTicket; // [S] blocks of the residual reduction done (0 between launches)
   double* resid;        // [S][kMaxResid] residual norm^2 per iteration (last slot: after the last)
   double* residC;       // [S][kMaxResid] contact residual norm^2, same slots
   double* c0;           // [S] |C(v_pred)|^2
