@@ -39,6 +39,9 @@ not physics.
 """
 from __future__ import annotations
 
+import json
+import os
+
 import numpy as np
 
 REL_TOL = 1e-4
@@ -179,5 +182,19 @@ def compare(s1, ref, ref64=None, has_pbf: bool = False, perturbed=None) -> dict:
         if report[f + "_gpu_vs_f64"] > floor or report[f] > floor + env:
             bad[f] = report[f]
     report.pop("_pert", None)
+    _record(report, bad)
     assert not bad, f"parity failure: {bad} (report {report})"
     return report
+
+
+def _record(report: dict, bad: dict) -> None:
+    """With XPBI_PARITY_REPORT=<file>, append this comparison's errors (GPU
+    vs f32 oracle, GPU vs f64 oracle, f32 oracle vs f64 oracle) as one JSON
+    line tagged with the running test."""
+    path = os.environ.get("XPBI_PARITY_REPORT")
+    if not path:
+        return
+    line = {"test": os.environ.get("PYTEST_CURRENT_TEST", "").split(" ")[0], "pass": not bad,
+            "errors": {k: float(v) for k, v in report.items()}}
+    with open(path, "a") as f:
+        f.write(json.dumps(line) + "\n")
