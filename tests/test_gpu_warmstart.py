@@ -57,9 +57,10 @@ def test_tracking_does_not_change_the_solve(xp, built_lib):
 @pytest.mark.parametrize("lanes,track", [(0, False), (1, False), (1, True)])
 def test_zero_network_is_the_previous_multiplier_start(xp, built_lib, lanes, track):
     """The network predicts an increment over the previous multiplier. With
-    one lane per slot and residual tracking the network mode's iteration 0
-    reads the constraint its features pass evaluated, the previous-multiplier
-    mode evaluates it in solveA: both must give the same bytes."""
+    one lane per slot the network mode's iteration 0 reads the constraint its
+    features pass evaluated (k_solveA_stored, with or without residual
+    tracking), the previous-multiplier mode evaluates it in solveA: both must
+    give the same bytes."""
     sc = xp.scenes.dam_breach()
     zero = np.zeros(9473, np.float32)
     res = []

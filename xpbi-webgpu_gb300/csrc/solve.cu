@@ -613,43 +613,19 @@ __device__ __forceinline__ void recordSolidDisp(const Bufs& b, uint32_t i, int k
 //   replaced by the plain start lambda0 = 0 (the plain solve stays the
 //   fallback). With lambda0 = 0 both updates are the reference's.
 // flags & kMeasureOnly: residual only (the pass after the last iteration).
-// flags & kStoredC (iteration 0, after the features pass; tracked instances):
-//   the constraint is the one the features pass evaluated at the same
-//   velocities. The plain instances keep their registers for the sweep.
+// flags & kStoredC (iteration 0, after the features pass, one lane per
+//   slot): the constraint is the one the features pass evaluated at the
+//   same velocities; k_solveA_stored applies it without a neighbour sweep.
 // G lanes per slot (G = 4 for small scenes): the lanes split the neighbour
 // sweep, lane 0 finishes the slot.
-template <bool kTrack, int kMinB, int G, int kBlock = kThreads>
-__global__ void __launch_bounds__(kBlock, kMinB) k_solveA(Bufs b, int k, const float4* __restrict__ velIn,
-                                                            int flags) {
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t i = t / G, lane = t % G;
-  if (i >= b.N) return;
-  const Ctx cx = ctxOf(b, i);
+//
+// The update of slot i from its constraint c (lane 0 of the slot).
+template <bool kTrack>
+__device__ __forceinline__ void solveAUpdate(const Bufs& b, const Ctx& cx, uint32_t i, const float4& pi,
+                                             const float4* __restrict__ velIn, uint32_t mi, const Constraint& c,
+                                             int k, bool warm0, bool measure) {
   const SceneDev& S = *cx.scene;
   constexpr bool track = kTrack;
-  const bool measure = kTrack && (flags & kMeasureOnly) != 0;  // measure passes are tracked ones
-  const bool warm0 = (flags & kWarm) != 0 && k == 0;
-  const float4 pi = b.posS[i];
-  const bool active = measure || (k < S.iterations && !sceneDone(b, i));
-  recordSolidDisp(b, i, k, active && !waterW(pi.w) && lane == 0 ? S.dt * length(xyz(velIn[i])) : 0.f);
-  if (!active || waterW(pi.w)) {  // water: its record is never read
-    if (track && lane == 0) {
-      b.rr[i] = 0.f;
-      if (k == 0) b.c0sq[i] = 0.f;
-    }
-    return;
-  }
-  const uint32_t mi = matOfW(pi.w);
-  const float st = b.stateS[i];
-  const MatDev m = hardenedMat(cx.mats[mi], st);
-  Constraint c;
-  if (kTrack && (flags & kStoredC) != 0 && k == 0) {  // the tracked (solver-mode) instances only
-    if (G > 1 && lane != 0) return;
-    c = loadConstraint(b, i);
-  } else {
-    c = evalConstraint<G>(b, cx, i, pi, velIn, m, st, lane);
-    if (G > 1 && lane != 0) return;
-  }
   const float g = S.kDamp;
   const float stiff = (1.f + g) * c.denom + S.alphaT;  // d(residual) / d(applied multiplier)
   const float r0 = c.C + g * S.dt * c.cdot;            // residual at lambda = 0
@@ -682,6 +658,58 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveA(Bufs b, int k, const f
   b.lam[i] = lam0 + dlam;
   const float imp = warm0 ? lam0 + dlam : dlam;
   storeSp(b, i, mscale(c.GL, imp), c.sgrad * imp, xi, xci, mass);
+}
+
+template <bool kTrack, int kMinB, int G, int kBlock = kThreads>
+__global__ void __launch_bounds__(kBlock, kMinB) k_solveA(Bufs b, int k, const float4* __restrict__ velIn,
+                                                            int flags) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t / G, lane = t % G;
+  if (i >= b.N) return;
+  const Ctx cx = ctxOf(b, i);
+  const SceneDev& S = *cx.scene;
+  constexpr bool track = kTrack;
+  const bool measure = kTrack && (flags & kMeasureOnly) != 0;  // measure passes are tracked ones
+  const bool warm0 = (flags & kWarm) != 0 && k == 0;
+  const float4 pi = b.posS[i];
+  const bool active = measure || (k < S.iterations && !sceneDone(b, i));
+  recordSolidDisp(b, i, k, active && !waterW(pi.w) && lane == 0 ? S.dt * length(xyz(velIn[i])) : 0.f);
+  if (!active || waterW(pi.w)) {  // water: its record is never read
+    if (track && lane == 0) {
+      b.rr[i] = 0.f;
+      if (k == 0) b.c0sq[i] = 0.f;
+    }
+    return;
+  }
+  const uint32_t mi = matOfW(pi.w);
+  const float st = b.stateS[i];
+  const MatDev m = hardenedMat(cx.mats[mi], st);
+  const Constraint c = evalConstraint<G>(b, cx, i, pi, velIn, m, st, lane);
+  if (G > 1 && lane != 0) return;
+  solveAUpdate<kTrack>(b, cx, i, pi, velIn, mi, c, k, warm0, measure);
+}
+
+// Iteration 0 after the features pass: the constraint that pass stored at
+// these velocities (bit-identical to evaluating it), no neighbour sweep — a
+// register-light launch at full occupancy in place of the sweep kernel.
+template <bool kTrack>
+__global__ void __launch_bounds__(kThreads) k_solveA_stored(Bufs b, const float4* __restrict__ velIn, int flags) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.N) return;
+  const Ctx cx = ctxOf(b, i);
+  const SceneDev& S = *cx.scene;
+  const bool warm0 = (flags & kWarm) != 0;
+  const float4 pi = b.posS[i];
+  const bool active = 0 < S.iterations && !sceneDone(b, i);
+  recordSolidDisp(b, i, 0, active && !waterW(pi.w) ? S.dt * length(xyz(velIn[i])) : 0.f);
+  if (!active || waterW(pi.w)) {
+    if (kTrack) {
+      b.rr[i] = 0.f;
+      b.c0sq[i] = 0.f;
+    }
+    return;
+  }
+  solveAUpdate<kTrack>(b, cx, i, pi, velIn, matOfW(pi.w), loadConstraint(b, i), 0, warm0, false);
 }
 
 // Network features of every slot at iteration 0 (zeros for water):
@@ -1305,6 +1333,13 @@ void solveAVariant(const Bufs& b, int k, const float4* velIn, int flags, cudaStr
         b, k, velIn, flags);
 }
 void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, int variant, int lanes, cudaStream_t st) {
+  if (flags & kStoredC) {  // iteration 0 after the features pass (one lane per slot)
+    if (flags & kTrackResid)
+      k_solveA_stored<true><<<grid(b.N), kThreads, 0, st>>>(b, velIn, flags);
+    else
+      k_solveA_stored<false><<<grid(b.N), kThreads, 0, st>>>(b, velIn, flags);
+    return;
+  }
   if (lanes == 4) {  // small scenes: four lanes per slot, the allocator's register choice
     const uint32_t threads = 4u * b.N;
     if (flags & kTrackResid)
