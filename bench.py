@@ -376,6 +376,22 @@ def run_xpbi(args, rank: int, world: int):
                 "algo_bytes_per_launch": algo, "solid_particles": n_solid, "water_particles": n_water,
                 "share": sum(per[dom]) / total_ms,
                 "kernel_ms": {k: round(statistics.mean(v), 4) for k, v in per.items()}}
+    # every kernel with a byte model: its algorithmic bytes per launch over its
+    # own event time; and the substep's (all launches' bytes over the graph's
+    # time per substep)
+    reps = max(1, args.profile_substeps)
+    kern, sub_bytes = {}, 0.0
+    for k, v in per.items():
+        if k not in ALGO_BYTES:
+            continue
+        b_s, b_w = ALGO_BYTES[k]
+        nbytes = b_s * n_solid + b_w * n_water
+        sub_bytes += nbytes * len(v) / reps
+        gbs = nbytes / (statistics.mean(v) / 1e3) / 1e9
+        kern[k] = {"launches_per_substep": len(v) // reps, "achieved": round(gbs, 1), "frac": round(gbs / peak, 4)}
+    roofline["kernels"] = kern
+    sub_gbs = sub_bytes / (ms / args.steps / 1e3) / 1e9
+    roofline["substep"] = {"algo_bytes": sub_bytes, "achieved": round(sub_gbs, 1), "frac": round(sub_gbs / peak, 4)}
     sim.close()
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
