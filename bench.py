@@ -385,7 +385,8 @@ def run_xpbi(args, rank: int, world: int):
         if k not in ALGO_BYTES:
             continue
         b_s, b_w = ALGO_BYTES[k]
-        nbytes = b_s * n_solid + b_w * n_water
+        # the scan moves 8 bytes per cell (cell counts in, starts out)
+        nbytes = 8 * sim.num_cells if k == "scan" else b_s * n_solid + b_w * n_water
         sub_bytes += nbytes * len(v) / reps
         gbs = nbytes / (statistics.mean(v) / 1e3) / 1e9
         kern[k] = {"launches_per_substep": len(v) // reps, "achieved": round(gbs, 1), "frac": round(gbs / peak, 4)}
