@@ -193,6 +193,14 @@ int xpbi_device_ptrs(xpbi_sim* sim, void** pos4, void** vel4, void** materials);
 /* Number of kernel launches one substep issues with this schedule. */
 int xpbi_launches_per_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t* out);
 
+/* Failure-path check (no counterpart in the reference): enqueues, on the
+ * handle's stream, the prefix scan's bounded look-back wait on a descriptor
+ * that nothing publishes. The wait gives up after `polls` polls (1..2^20,
+ * ~0.1 us each) and raises the device error word, so the next
+ * xpbi_synchronize returns XPBI_ERR_DEVICE and clears it; the handle stays
+ * usable. No kernel faults, traps or waits without a limit. */
+int xpbi_test_wait_expiry(xpbi_sim* sim, uint32_t polls);
+
 /* ---- headless renderer (web/js/shaders/render.js, main.js:232-272) ----
  * The reference draws each frame through WebGPU: the ground plane with its
  * grid, the domain box, and every particle as a depth-correct sphere

@@ -30,7 +30,7 @@ EXPORTS = (
     "xpbi_mlp_param_count", "xpbi_mlp_forward", "xpbi_mlp_grad", "xpbi_mlp_train",
     "xpbi_set_solver", "xpbi_set_network", "xpbi_read_residuals", "xpbi_read_training",
     "xpbi_sort_cells_noalloc", "xpbi_read_contact_residuals", "xpbi_autotune", "xpbi_set_variants",
-    "xpbi_render", "xpbi_set_lanes", "xpbi_read_positions_async",
+    "xpbi_render", "xpbi_set_lanes", "xpbi_read_positions_async", "xpbi_test_wait_expiry",
 )
 
 
@@ -98,6 +98,7 @@ _SIGS = {
                                        C.c_char_p, C.c_size_t]),
     "xpbi_device_ptrs": (C.c_int, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
     "xpbi_launches_per_substep": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
+    "xpbi_test_wait_expiry": (C.c_int, [_P, C.c_uint32]),
     "xpbi_mlp_param_count": (C.c_int, []),
     "xpbi_mlp_forward": (C.c_int, [_F32P, C.c_uint32, _F32P, _F32P]),
     "xpbi_mlp_grad": (C.c_int, [_F32P, _F32P, C.c_uint32, _F32P, _F32P, _F32P]),

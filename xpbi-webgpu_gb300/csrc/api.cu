@@ -649,6 +649,7 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   A(b.scenes, nScenes);
   A(b.mats, (size_t)nScenes * kMaxMats);
   A(b.err, 1);
+  A(b.waitProbe, 1);
   A(s->matWords, (size_t)nScenes * kMaxMats * XPBI_MATERIAL_WORDS);
 #undef A
   // initial state (sim.js:52-81)
@@ -680,7 +681,8 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   bool ok = H2D(b.pos, pos.data(), 16 * n) && H2D(b.vel, vel.data(), 16 * n) && H2D(b.F, F.data(), 36 * n) &&
             H2D(b.state, state.data(), 4 * n) && H2D(b.lam, zero.data(), 4 * n) &&
             H2D(b.pbfLam, zero.data(), 4 * n) && H2D(b.sceneOf, sceneOf.data(), 2 * n) &&
-            cudaMemset(b.err, 0, sizeof(int)) == cudaSuccess && cudaMemset(b.L, 0, 36 * n) == cudaSuccess &&
+            cudaMemset(b.err, 0, sizeof(int)) == cudaSuccess &&
+            cudaMemset(b.waitProbe, 0, sizeof(unsigned long long)) == cudaSuccess && cudaMemset(b.L, 0, 36 * n) == cudaSuccess &&
             cudaMemset(b.sortedIdx, 0, 4 * n) == cudaSuccess && cudaMemset(b.lamOut, 0, 4 * n) == cudaSuccess &&
             cudaMemset(b.lamPrev, 0, 4 * n) == cudaSuccess && cudaMemset(b.lamWarm, 0, 4 * n) == cudaSuccess &&
             cudaMemset(b.done, 0, sizeof(int) * nScenes) == cudaSuccess &&
@@ -1383,6 +1385,14 @@ int xpbi_read_training(xpbi_sim* sim, uint32_t scene, float* features16, float* 
     for (size_t i = 0; i < n; ++i) target[i] *= aT;
   }
   if (alpha_tilde) *alpha_tilde = aT;
+  return XPBI_OK;
+}
+
+int xpbi_test_wait_expiry(xpbi_sim* sim, uint32_t polls) {
+  XPBI_TRY(checkSim(sim));
+  if (polls < 1u || polls > (1u << 20)) return fail(XPBI_ERR_INVALID, "polls must be 1..1048576");
+  launch_wait_expiry(sim->b, sim->b.waitProbe, polls, sim->stream);
+  XPBI_CK(cudaGetLastError());
   return XPBI_OK;
 }
 

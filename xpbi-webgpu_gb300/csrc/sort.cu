@@ -61,6 +61,23 @@ __global__ void __launch_bounds__(kThreads) k_count(Bufs b) {
   if (lane == __ffs(peers) - 1) atomicAdd(&b.cursor[key], (uint32_t)__popc(peers));
 }
 
+// Bounded wait for a look-back descriptor: polls `slot` until its flag
+// (high word) is nonzero and returns the descriptor; after `polls` empty
+// polls it raises kErrLookback in the error word and returns 0 (no flag),
+// and the caller goes on. Nothing waits without a limit.
+__device__ __forceinline__ unsigned long long waitDescriptor(const volatile unsigned long long* slot,
+                                                             uint32_t polls, int* err) {
+  for (uint32_t spins = 0;; ++spins) {
+    const unsigned long long w64 = *slot;
+    if ((uint32_t)(w64 >> 32) != 0u) return w64;
+    if (spins >= polls) {
+      atomicOr(err, kErrLookback);
+      return 0ull;
+    }
+    __nanosleep(64);
+  }
+}
+
 // Exclusive scan of the C counts (plus one zero item, whose prefix is the
 // N sentinel) into cellStart[0..C] and cursor[0..C-1]. Tiles take a ticket
 // in launch order and look back over earlier tiles' descriptors; a tile only
@@ -119,18 +136,10 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Bufs b) {
       } else {
         atomicExch(b.tileStatus + tile, (1ull << 32) | agg);
         int pred = (int)tile - 1;
-        uint32_t spins = 0;
         while (pred >= 0) {
-          unsigned long long w64 = status[pred];
-          uint32_t flag = (uint32_t)(w64 >> 32);
-          if (flag == 0u) {
-            if (++spins > kLookbackSpinLimit) {
-              atomicOr(b.err, kErrLookback);
-              break;
-            }
-            __nanosleep(64);
-            continue;
-          }
+          const unsigned long long w64 = waitDescriptor(status + pred, kLookbackSpinLimit, b.err);
+          const uint32_t flag = (uint32_t)(w64 >> 32);
+          if (flag == 0u) break;  // the wait expired (error word raised)
           excl += (uint32_t)w64;
           if (flag == 2u) break;
           --pred;
@@ -260,6 +269,14 @@ __global__ void __launch_bounds__(kThreads) k_reorder(Bufs b, int keepLam) {
 
 inline unsigned grid(uint32_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
+// Test hook: the scan's bounded wait on a descriptor nothing publishes
+// (`slot` stays zero), so the wait expires after `polls` polls and raises
+// the error word the host reads — the failure path of the look-back without
+// a fault. One thread.
+__global__ void k_wait_expiry(Bufs b, const unsigned long long* slot, uint32_t polls) {
+  waitDescriptor(slot, polls, b.err);
+}
+
 }  // namespace
 
 uint32_t scan_tiles(uint32_t cells) { return (cells + 1 + kScanTile - 1) / kScanTile; }
@@ -268,6 +285,9 @@ void launch_count(const Bufs& b, cudaStream_t st) {
   cudaMemsetAsync(b.cursor, 0, sizeof(uint32_t) * b.C, st);
   cudaMemsetAsync(b.cellWater, 0, b.C, st);
   k_count<<<grid(b.N, kThreads), kThreads, 0, st>>>(b);
+}
+void launch_wait_expiry(const Bufs& b, const unsigned long long* slot, uint32_t polls, cudaStream_t st) {
+  k_wait_expiry<<<1, 1, 0, st>>>(b, slot, polls);
 }
 void launch_scan(const Bufs& b, cudaStream_t st) {
   // ticket, crowded-cell count and tile descriptors are contiguous: one

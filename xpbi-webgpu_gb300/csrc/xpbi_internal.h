@@ -144,6 +144,7 @@ struct Bufs {
   SceneDev* scenes;     // [S]
   MatDev* mats;         // [S * 8]
   int* err;             // [1] device error word
+  unsigned long long* waitProbe;  // [1] a descriptor nothing publishes (xpbi_test_wait_expiry)
   uint32_t N, C, S;
   uint32_t scanTiles;
 };
@@ -151,6 +152,7 @@ struct Bufs {
 // ---- launchers (sort.cu) ----
 void launch_count(const Bufs& b, cudaStream_t st);
 void launch_scan(const Bufs& b, cudaStream_t st);
+void launch_wait_expiry(const Bufs& b, const unsigned long long* slot, uint32_t polls, cudaStream_t st);
 void launch_scatter(const Bufs& b, cudaStream_t st);
 void launch_reorder(const Bufs& b, bool keepLam, cudaStream_t st);
 void launch_warm_from_prev(const Bufs& b, cudaStream_t st);

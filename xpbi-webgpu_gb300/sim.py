@@ -198,6 +198,12 @@ class Simulation:
         check(lib().xpbi_launches_per_substep(self._h, iterations, 1 if has_water else 0, C.byref(out)))
         return out.value
 
+    def test_wait_expiry(self, polls: int = 1000):
+        """Enqueue the scan's bounded wait on a descriptor nothing publishes:
+        the next synchronize() raises XpbiError (ERR_DEVICE) and the handle
+        stays usable."""
+        check(lib().xpbi_test_wait_expiry(self._h, polls))
+
     # -- readback (main.js:291-312) and state access
     def read_pos(self, scene: int = 0, out=None):
         n = self.scene_sizes[scene]
