@@ -16,6 +16,7 @@ Arms:
 from __future__ import annotations
 
 import argparse
+import datetime
 import importlib
 import json
 import os
@@ -74,45 +75,56 @@ def workload(name: str, rank: int = 0):
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling during the timed region: samples every 50 ms,
+    started before the region (the sampler needs a moment to come up) and
+    kept only where their timestamps fall inside it."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index: int):
         self.index = index
         self.p = None
+        self.t0 = self.t1 = 0.0
 
     def start(self):
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "50"],
                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.p = None
+        time.sleep(0.3)
+        self.t0 = time.time()
 
     def stop(self) -> dict:
+        self.t1 = time.time()
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.p.terminate()
         out, _ = self.p.communicate(timeout=10)
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        return self.summarise(out, self.t0, self.t1)
+
+    @staticmethod
+    def summarise(out: str, t0: float, t1: float) -> dict:
+        rows = []
         for line in out.splitlines():
             f = [x.strip() for x in line.split(",")]
-            if len(f) < 9:
+            if len(f) < 10:
                 continue
             try:
-                sm.append(float(f[1]))
-                mx.append(float(f[2]))
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((ts, float(f[2]), float(f[3]), f[6:10]))
             except ValueError:
                 continue
-            for k, n in enumerate(names):
-                if f[5 + k].lower().startswith("active"):
-                    reasons.add(n)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        inside = [r for r in rows if t0 - 0.05 <= r[0] <= t1 + 0.05]
+        use = inside or rows
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = {n for r in use for n, v in zip(names, r[3]) if v.lower().startswith("active")}
+        return {"sm_mhz": statistics.median(r[1] for r in use) if use else None,
+                "sm_max_mhz": max(r[2] for r in use) if use else None,
+                "reasons": sorted(reasons), "samples": len(use), "samples_in_region": len(inside)}
 
 
 def cpu_path():
