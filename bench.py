@@ -59,8 +59,11 @@ NCU_TRAFFIC_PER_PARTICLE = {"solveB": 127.8, "solveA": 153.7, "pbfA": 105.6, "co
 
 def workload(name: str, rank: int = 0):
     xp = importlib.import_module("xpbi-webgpu_gb300")
-    if name == "dam_mix4":
-        scenes = xp.scenes.config_dam_mix(seeds=tuple(4 * rank + k for k in range(4)))
+    if name.startswith("dam_mix") and name[7:].isdigit() and int(name[7:]) > 0:
+        # dam_mix<S>: S one-million-particle dam breaches in one handle
+        # (dam_mix4 is the 4M benchmark mix; larger S fill more of the HBM)
+        count = int(name[7:])
+        scenes = xp.scenes.config_dam_mix(seeds=tuple(count * rank + k for k in range(count)))
     elif name == "dam_breach":
         scenes = [xp.scenes.config_dam_breach(seed=rank)]
     elif name == "nacc_snowball":
