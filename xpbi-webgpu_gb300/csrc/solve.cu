@@ -339,7 +339,9 @@ __device__ __forceinline__ void bonetLok(const Bufs& b, const Ctx& cx, uint32_t 
 // candidate walk records the substep's neighbour list.
 template <bool kSums>
 __global__ void XPBI_LB_COMPUTEL k_computeL(Bufs b) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  // blocks run last to first: the pass starts where the reorder ended, on
+  // slots whose data is still in L2
+  const uint32_t i = (gridDim.x - 1u - blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
@@ -951,7 +953,9 @@ struct SBData {
 template <int kMinB, int G, int kBlock = kThreads>
 __global__ void __launch_bounds__(kBlock, kMinB) k_solveB(Bufs b, int k, const float4* __restrict__ velIn,
                                                       float4* __restrict__ velOut, int writeXc, int flags) {
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  // blocks run last to first: the pass starts where solveA ended, on slots
+  // whose data is still in L2
+  const uint32_t t = (gridDim.x - 1u - blockIdx.x) * blockDim.x + threadIdx.x;
   const uint32_t i = t / G, lane = t % G;
   for (uint32_t q = t; q < b.S; q += gridDim.x * blockDim.x)  // the next iteration's slot
     b.solidDisp[(size_t)((k + 1) & 1) * b.S + q] = 0u;
@@ -1190,7 +1194,9 @@ struct PBData {
 // record of predicted neighbours.
 __global__ void XPBI_LB_PBF k_pbfB(Bufs b, int k, const float4* __restrict__ velIn,
                                                     float4* __restrict__ velOut) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  // blocks run last to first: the pass starts where pbfA ended, on
+  // slots whose data is still in L2
+  const uint32_t i = (gridDim.x - 1u - blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
@@ -1282,7 +1288,9 @@ __global__ void XPBI_LB_UPDATE k_xsph(Bufs b, const float4* __restrict__ velIn,
 // clamp and position update (simkernels.js:528-542). Outputs go to the
 // "current" arrays, so neighbours still read the unclamped sorted inputs.
 __global__ void XPBI_LB_UPDATE k_updateF_integrate(Bufs b, const float4* __restrict__ velIn) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  // blocks run last to first: the pass starts where xsph ended, on
+  // slots whose data is still in L2
+  const uint32_t i = (gridDim.x - 1u - blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
