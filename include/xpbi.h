@@ -350,6 +350,25 @@ int xpbi_mlp_train(const float* X, const float* T, uint32_t rows, float* params,
 int xpbi_sort_cells_noalloc(const float* pos4, uint32_t n, const float origin[3], float cell_size,
                             const int32_t dims[3], uint32_t* cell_start, uint32_t* sorted_idx, void* cuda_stream);
 
+/* Status of the last xpbi_sort_cells_noalloc call on the current device
+ * (no counterpart in the reference). Its prefix scan waits, with a bounded
+ * number of polls, for earlier tiles to publish their sums; a wait that runs
+ * out raises an error word inside the same fixed scratch array, and the
+ * outputs of that call are then not valid. This synchronises cuda_stream
+ * (the stream the sort was enqueued on), reads the word and clears it:
+ * XPBI_OK, or XPBI_ERR_DEVICE with the word in xpbi_last_error(). It
+ * allocates nothing. The next sort call clears the word itself, so ask
+ * before making it. */
+int xpbi_sort_cells_noalloc_status(void* cuda_stream);
+
+/* Failure-path check of the above (no counterpart in the reference): runs
+ * the scan's bounded look-back wait on a descriptor of the fixed scratch
+ * array that nothing publishes, with a limit of `polls` polls (1..2^20,
+ * ~0.1 us each), on cuda_stream. The wait gives up and raises the error word
+ * that xpbi_sort_cells_noalloc_status reports. Nothing faults or waits
+ * without a limit. */
+int xpbi_test_noalloc_wait_expiry(uint32_t polls, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -14,8 +14,9 @@ with the working tree so the library can be rebuilt on another host):
     xpbi_wgsl.inc      the translated shader module
     libxpbi_wgslref.so the reference kernels behind wr_substep()
 
-translate() needs the reference checkout (XPBI_REFERENCE, default
-/root/reference); build() needs only the generated source.
+translate() needs the reference checkout: the directory XPBI_REFERENCE
+names, else a checkout named `reference` beside this repository; build()
+needs only the generated source.
 """
 from __future__ import annotations
 
@@ -35,7 +36,12 @@ SHADERS = ("web/js/shaders/common.js", "web/js/shaders/simkernels.js")
 
 
 def reference_root() -> str:
-    return os.environ.get("XPBI_REFERENCE", "/root/reference")
+    """The reference checkout: XPBI_REFERENCE, else `reference` beside this
+    repository's root."""
+    env = os.environ.get("XPBI_REFERENCE")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 
 # ------------------------------------------------------------------ extraction

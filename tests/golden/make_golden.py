@@ -1,7 +1,8 @@
 """Generate golden vectors from the reference's own NumPy prototype.
 
-Reads prototype/xpbi2d.py of Chiplis/xpbi-webgpu (path given as argv[1],
-default /root/reference), extracts its `drucker_prager` (xpbi2d.py:93-108)
+Reads prototype/xpbi2d.py of Chiplis/xpbi-webgpu (checkout given as
+argv[1], else XPBI_REFERENCE, else `reference` beside this repository),
+extracts its `drucker_prager` (xpbi2d.py:93-108)
 and `stvk_psi_and_dpsi` (xpbi2d.py:110-116) with `ast` — the script's
 simulation loop is not executed — and evaluates them with the dimension
 set to 3 (the functions are written for any `d`) on seeded singular-value
@@ -36,7 +37,9 @@ def load_functions(ref_root: str):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    repo = os.path.dirname(os.path.dirname(HERE))
+    ref_root = (sys.argv[1] if len(sys.argv) > 1 else
+                os.environ.get("XPBI_REFERENCE") or os.path.join(os.path.dirname(repo), "reference"))
     mod = load_functions(ref_root)
     rng = np.random.default_rng(2024)
     cases = []

@@ -57,9 +57,14 @@ def _two_calls(torch, inputs, grid):
         si_out = torch.full((n,), -1, dtype=torch.int32, device="cuda")
         rc = _call(p.data_ptr(), n, origin, cs, dims, cs_out.data_ptr(), si_out.data_ptr(), stream)
         assert rc == 0, _abi().lib().xpbi_last_error()
+        assert _status(stream) == 0, _abi().lib().xpbi_last_error()  # no wait ran out
         outs.append((p, cs_out, si_out))
     torch.cuda.synchronize()
     return [(c.cpu().numpy().view(np.uint32), s.cpu().numpy().view(np.uint32)) for _, c, s in outs]
+
+
+def _status(stream):
+    return _abi().lib().xpbi_sort_cells_noalloc_status(C.c_void_p(stream))
 
 
 @pytest.mark.gpu
@@ -124,6 +129,10 @@ def test_noalloc_sort_rejects_out_of_range(xp, built_lib):
         (fake, MAX_N + 1, dims, fake, fake),             # too many particles
         (fake, 0, dims, fake, fake),                     # nothing to sort
         (fake, 16, np.array([1024, 1024, 2], np.int32), fake, fake),  # too many cells
+        # products that wrap a 64-bit (or 32-bit) count if formed before the check
+        (fake, 16, np.array([1 << 22, 1 << 22, 1 << 20], np.int32), fake, fake),
+        (fake, 16, np.array([2**31 - 1] * 3, np.int32), fake, fake),
+        (fake, 16, np.array([1 << 16, 1 << 16, 1], np.int32), fake, fake),
         (fake, 16, np.array([0, 8, 8], np.int32), fake, fake),        # empty grid
         (fake + 4, 16, dims, fake, fake),                # misaligned positions
         (fake, 16, dims, fake + 4, fake),                # misaligned cell starts
@@ -134,3 +143,32 @@ def test_noalloc_sort_rejects_out_of_range(xp, built_lib):
         assert rc == abi.ERR_INVALID, (n, d)
         assert abi.lib().xpbi_last_error()
     assert _call(fake, 16, origin, 0.0, dims, fake, fake, 0) == abi.ERR_INVALID
+
+
+@pytest.mark.gpu
+def test_noalloc_expired_wait_is_reported(xp, built_lib):
+    """A bounded look-back wait that runs out inside the fixed scratch array
+    reaches the caller through xpbi_sort_cells_noalloc_status (not as a
+    silently wrong permutation), the word is cleared, and the next sort runs
+    as before. The wait is the scan's own helper on a descriptor nothing
+    publishes, with a short limit: nothing faults or spins without one."""
+    torch = pytest.importorskip("torch")
+    abi = _abi()
+    stream = torch.cuda.current_stream().cuda_stream
+    sc = xp.scenes.config_dam_breach(scale=0.05)
+    with xp.Simulation(sc) as sim:
+        sim.write_params(xp.params_for(sc))
+        grid = _grid(sim)
+        sim.encode_substep(sc["iterations"], sc["hasWater"])
+        st = sim.read_state()
+    pos = st["pos"]
+    assert abi.lib().xpbi_test_noalloc_wait_expiry(1000, C.c_void_p(stream)) == 0
+    assert _status(stream) == abi.ERR_DEVICE
+    assert b"look-back" in abi.lib().xpbi_last_error()
+    assert _status(stream) == 0  # read and cleared
+    want, _ = _sorted_by_rule(pos, *grid)
+    (cell_start, sorted_idx), = _two_calls(torch, [pos], grid)
+    assert np.array_equal(sorted_idx, want)
+    assert cell_start[-1] == len(pos)
+    for bad in (0, (1 << 20) + 1):
+        assert abi.lib().xpbi_test_noalloc_wait_expiry(bad, C.c_void_p(stream)) == abi.ERR_INVALID

@@ -31,6 +31,7 @@ EXPORTS = (
     "xpbi_set_solver", "xpbi_set_network", "xpbi_read_residuals", "xpbi_read_training",
     "xpbi_sort_cells_noalloc", "xpbi_read_contact_residuals", "xpbi_autotune", "xpbi_set_variants",
     "xpbi_render", "xpbi_set_lanes", "xpbi_read_positions_async", "xpbi_test_wait_expiry",
+    "xpbi_sort_cells_noalloc_status", "xpbi_test_noalloc_wait_expiry",
 )
 
 
@@ -115,6 +116,8 @@ _SIGS = {
     "xpbi_render": (C.c_int, [_P, C.c_uint32, C.POINTER(Camera), C.c_uint32, C.c_uint32, C.POINTER(C.c_uint8),
                               C.POINTER(_P)]),
     "xpbi_sort_cells_noalloc": (C.c_int, [_P, C.c_uint32, _F32P, C.c_float, C.POINTER(C.c_int32), _P, _P, _P]),
+    "xpbi_sort_cells_noalloc_status": (C.c_int, [_P]),
+    "xpbi_test_noalloc_wait_expiry": (C.c_int, [C.c_uint32, _P]),
 }
 
 

@@ -19,9 +19,17 @@
 // the last call's contents, so every call clears what must start at zero, and
 // calls whose work overlaps on the GPU (different streams, or different host
 // threads on one device) race on it: serialise them.
+//
+// The prefix scan's look-back waits are bounded; one that runs out raises an
+// error word inside the same array instead of the sort's outputs telling
+// anything. xpbi_sort_cells_noalloc_status synchronises the caller's stream
+// and reports (and clears) that word, so a caller learns of an expired wait
+// without any allocation. The next sort call clears the word itself, so the
+// status belongs to the last call made before it.
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -54,7 +62,8 @@ constexpr uint32_t wScene = wCtl + al(2 * (kMaxTiles + 1));
 constexpr uint32_t wMats = wScene + al((sizeof(SceneDev) + 3) / 4);
 constexpr uint32_t wCellWater = wMats + al((kMaxMats * sizeof(MatDev) + 3) / 4);
 constexpr uint32_t wErr = wCellWater + al(kMaxCells / 4 + 4);
-constexpr uint32_t kWords = wErr + 64;
+constexpr uint32_t wProbe = wErr + 64;  // a descriptor nothing publishes (xpbi_test_noalloc_wait_expiry)
+constexpr uint32_t kWords = wProbe + 64;
 
 static __device__ __align__(256) uint32_t g_sortScratch[kWords];
 
@@ -123,14 +132,17 @@ extern "C" int xpbi_sort_cells_noalloc(const float* pos4, uint32_t n, const floa
     return setError(XPBI_ERR_INVALID, "particle count must be 1.." + std::to_string(kMaxParticles) +
                                           " for the allocation-free sort");
   if (!(cell_size > 0.f)) return setError(XPBI_ERR_INVALID, "cell_size must be positive");
+  for (int k = 0; k < 3; ++k)
+    if (dims[k] < 1) return setError(XPBI_ERR_INVALID, "grid dimensions must be positive");
+  // checked after every factor: the running product stays <= kMaxCells
+  // (2^20) before each multiplication by a factor < 2^31, so it cannot wrap
   uint64_t cells = 1;
   for (int k = 0; k < 3; ++k) {
-    if (dims[k] < 1) return setError(XPBI_ERR_INVALID, "grid dimensions must be positive");
     cells *= (uint64_t)dims[k];
+    if (cells > kMaxCells)
+      return setError(XPBI_ERR_INVALID, "grid has more than " + std::to_string(kMaxCells) +
+                                            " cells, the allocation-free sort's limit");
   }
-  if (cells > kMaxCells)
-    return setError(XPBI_ERR_INVALID, "grid has more than " + std::to_string(kMaxCells) +
-                                          " cells, the allocation-free sort's limit");
   uint32_t* base = nullptr;
   int rc = scratchAddress(&base);
   if (rc != XPBI_OK) return rc;
@@ -172,6 +184,44 @@ extern "C" int xpbi_sort_cells_noalloc(const float* pos4, uint32_t n, const floa
   const uint32_t big = launch_bigcells(b, base + wBigScratch, st);
   k_rank_only<<<(n + 255) / 256, 256, 0, st>>>(b.tmp, b.key, b.cellStart, n, big, sorted_idx);
   cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return setError(XPBI_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+  return XPBI_OK;
+}
+
+extern "C" int xpbi_sort_cells_noalloc_status(void* cuda_stream) {
+  uint32_t* base = nullptr;
+  int rc = scratchAddress(&base);
+  if (rc != XPBI_OK) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+  int err = 0;
+  cudaError_t e = cudaMemcpyAsync(&err, base + wErr, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return setError(XPBI_ERR_CUDA, std::string("status read: ") + cudaGetErrorString(e));
+  if (err == 0) return XPBI_OK;
+  e = cudaMemsetAsync(base + wErr, 0, sizeof(int), st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return setError(XPBI_ERR_CUDA, std::string("status clear: ") + cudaGetErrorString(e));
+  return setError(XPBI_ERR_DEVICE, "allocation-free sort: device error word 0x" + [&] {
+    char t[16];
+    std::snprintf(t, sizeof(t), "%x", (unsigned)err);
+    return std::string(t);
+  }() + " (bounded look-back wait expired; cell_start and sorted_idx are not valid)");
+}
+
+extern "C" int xpbi_test_noalloc_wait_expiry(uint32_t polls, void* cuda_stream) {
+  if (polls < 1u || polls > (1u << 20)) return setError(XPBI_ERR_INVALID, "polls must be 1..1048576");
+  uint32_t* base = nullptr;
+  int rc = scratchAddress(&base);
+  if (rc != XPBI_OK) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+  Bufs b;
+  std::memset(&b, 0, sizeof(b));
+  b.err = reinterpret_cast<int*>(base + wErr);
+  unsigned long long* probe = reinterpret_cast<unsigned long long*>(base + wProbe);
+  cudaError_t e = cudaMemsetAsync(probe, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return setError(XPBI_ERR_CUDA, std::string("probe clear: ") + cudaGetErrorString(e));
+  launch_wait_expiry(b, probe, polls, st);
+  e = cudaGetLastError();
   if (e != cudaSuccess) return setError(XPBI_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
   return XPBI_OK;
 }

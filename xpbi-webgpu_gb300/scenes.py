@@ -35,12 +35,33 @@ def sample_box(rng, out, mid, states, lo, hi, h, mat_idx, jitter=0.2, state0=0.0
     states.append(np.full(len(base), state0, np.float64))
 
 
+def js_hypot3(a, b, c):
+    """Math.hypot(a, b, c) as the reference's browser (Chrome's V8) evaluates
+    it, elementwise in f64: the arguments scaled by the largest magnitude,
+    their squares added with Kahan compensation, sqrt(sum) * max. Lattice
+    points exactly on a sphere's surface (d == r up to rounding) land inside
+    or outside by this rounding, so the membership test uses it rather than
+    sqrt(a^2 + b^2 + c^2), which differs on ~1e-4 of the snowball's points."""
+    v = [np.abs(np.asarray(x, np.float64)) for x in (a, b, c)]
+    m = np.maximum(np.maximum(v[0], v[1]), v[2])
+    safe = np.where(m > 0, m, 1.0)
+    total = np.zeros_like(m)
+    comp = np.zeros_like(m)
+    for x in v:
+        n = x / safe
+        summand = n * n - comp
+        prelim = total + summand
+        comp = (prelim - total) - summand
+        total = prelim
+    return np.where(m > 0, np.sqrt(total) * m, 0.0)
+
+
 def sample_sphere(rng, out, mid, states, c, r, h, mat_idx, jitter=0.2, state0=0.0):
     """Lattice points inside a sphere with uniform jitter (scenes.js:22-38)."""
     n = math.ceil(2 * r / h)
     k, j, i = np.meshgrid(np.arange(n + 1), np.arange(n + 1), np.arange(n + 1), indexing="ij")
     p = np.stack([c[0] - r + i.ravel() * h, c[1] - r + j.ravel() * h, c[2] - r + k.ravel() * h], axis=1)
-    d = np.sqrt(((p - np.asarray(c)) ** 2).sum(axis=1))
+    d = js_hypot3(p[:, 0] - c[0], p[:, 1] - c[1], p[:, 2] - c[2])
     p = p[d <= r]
     p = p + (rng.random(p.shape) - 0.5) * jitter * h
     out.append(p)
