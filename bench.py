@@ -57,24 +57,32 @@ ALGO_BYTES = {"solveA": (196, 16), "solveB": (128, 48), "pbfA": (36, 36), "pbfB"
 NCU_TRAFFIC_PER_PARTICLE = {"solveB": 127.8, "solveA": 153.7, "pbfA": 105.6, "computeL": 229.5}
 
 
-def workload(name: str, rank: int = 0):
+def workload(name: str, rank: int = 0, world: int = 1):
+    """(package, this rank's scenes, scaling) of a named workload. The job's
+    batch is built once and split across ranks by the particle-count
+    bin-pack of shard.py (disjoint shards, no data-path collective):
+      dam_mix<S>   S one-million-particle dam breaches per rank (seeds
+                   0..S*world-1; dam_mix4 is the 4M benchmark mix): weak
+      batch256     the 256-scene mixed batch (seed 0), fixed in total: strong
+      dam_breach, nacc_snowball, sand_column   one scene per rank (seed =
+                   rank): weak"""
     xp = importlib.import_module("xpbi-webgpu_gb300")
+    shard = importlib.import_module("xpbi-webgpu_gb300.shard")
     if name.startswith("dam_mix") and name[7:].isdigit() and int(name[7:]) > 0:
-        # dam_mix<S>: S one-million-particle dam breaches in one handle
-        # (dam_mix4 is the 4M benchmark mix; larger S fill more of the HBM)
         count = int(name[7:])
-        scenes = xp.scenes.config_dam_mix(seeds=tuple(count * rank + k for k in range(count)))
-    elif name == "dam_breach":
+        batch = xp.scenes.config_dam_mix(seeds=tuple(range(count * world)))
+        return xp, shard.shard(batch, rank, world), "weak"
+    if name == "batch256":
+        return xp, shard.shard(xp.scenes.config_batch(seed=0), rank, world), "strong"
+    if name == "dam_breach":
         scenes = [xp.scenes.config_dam_breach(seed=rank)]
     elif name == "nacc_snowball":
         scenes = [xp.scenes.config_nacc_snowball(seed=rank)]
     elif name == "sand_column":
         scenes = [xp.scenes.config_sand_column(seed=rank)]
-    elif name == "batch256":
-        scenes = xp.scenes.config_batch(seed=rank)
     else:
         raise SystemExit(f"unknown workload {name}")
-    return xp, scenes
+    return xp, scenes, "weak"
 
 
 class Clocks:
@@ -130,6 +138,18 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(use), "samples_in_region": len(inside)}
 
 
+def standalone_scenes():
+    """scenes.py (the seeded scene factories, NumPy only) loaded by file path,
+    without importing the package, so the CPU leg touches no part of the
+    library under test."""
+    import importlib.util
+    path = os.path.join(ROOT, "xpbi-webgpu_gb300", "scenes.py")
+    spec = importlib.util.spec_from_file_location("xpbi_cpu_scenes", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def cpu_path():
     """(kind, substep function, description) of the CPU path timed beside
     the GPU: the reference's own kernels (its WGSL translated to C++ by
@@ -145,28 +165,58 @@ def cpu_path():
     return "port", O.substep, "f32 oracle port"
 
 
-def cpu_baseline(sample_scale: float, threads: int, substeps: int = 1, budget_s: float = 0.0):
-    """The CPU path on the host cores over a bounded sample of the workload:
-    one dam-breach scene with its z extent scaled by sample_scale, `substeps`
-    consecutive substeps from rest (with budget_s > 0: stop once that much
-    time has been spent, after at least one). Returns (particle-substeps/s,
-    particles, seconds, substeps run, kind, description)."""
-    from oracle import oracle as O
-    kind, fn, desc = cpu_path()
-    xp = importlib.import_module("xpbi-webgpu_gb300")
-    sc = xp.scenes.config_dam_breach(seed=0, scale=sample_scale)
-    pw, mw = xp.pack_uniforms(sc, xp.params_for(sc))
-    st = O.initial_state(sc)
-    n = len(sc["positions"])
+def cpu_sample_name(scale: float, preroll: int) -> str:
+    return f"dam_breach scale {scale:g} seed 0 after {preroll} plain substeps"
+
+
+class CpuSample:
+    """The CPU path on the benchmark's sample: one dam-breach scene (seed 0)
+    with its z extent scaled by `scale`, rolled `preroll` plain substeps
+    forward by the CPU path itself (the state the GPU workload's scenes are
+    timed from, at a size the host cores finish in minutes). Uniforms come
+    from oracle/uniforms.py and scenes from scenes.py loaded standalone: no
+    part of libxpbi runs here."""
+
+    def __init__(self, scale: float, preroll: int, threads: int):
+        from oracle import oracle as O
+        from oracle import uniforms as U
+        self.kind, self.fn, self.desc = cpu_path()
+        S = standalone_scenes()
+        sc = S.config_dam_breach(seed=0, scale=scale)
+        self.pw, self.mw = U.pack(sc, U.frame_params(sc))
+        self.it, self.pbf = sc["iterations"], sc["pbfIterations"]
+        self.n = len(sc["positions"])
+        self.threads = threads
+        self.name = cpu_sample_name(scale, preroll)
+        t0 = time.perf_counter()
+        self.st = O.initial_state(sc)
+        if preroll:
+            self.st = self.fn(self.pw, self.mw, self.st, self.it, True, self.pbf, substeps=preroll,
+                              threads=threads)
+        self.preroll_s = time.perf_counter() - t0
+
+    def step(self) -> float:
+        """One substep from the current state; returns its seconds."""
+        t0 = time.perf_counter()
+        self.st = self.fn(self.pw, self.mw, self.st, self.it, True, self.pbf, substeps=1, threads=self.threads)
+        return time.perf_counter() - t0
+
+
+def cpu_baseline(scale: float, preroll: int, threads: int, substeps: int, budget_s: float):
+    """Consecutive substeps of the CPU sample until `substeps` ran or
+    budget_s seconds were spent (at least one). Returns (particle-substeps/s,
+    cpu_baseline dict)."""
+    smp = CpuSample(scale, preroll, threads)
     dt, done = 0.0, 0
     while done < substeps:
-        t0 = time.perf_counter()
-        st = fn(pw, mw, st, sc["iterations"], True, sc["pbfIterations"], substeps=1, threads=threads)
-        dt += time.perf_counter() - t0
+        dt += smp.step()
         done += 1
         if budget_s > 0 and dt >= budget_s:
             break
-    return n * done / dt, n, dt, done, kind, desc
+    v = smp.n * done / dt
+    return v, {"value": v, "unit": UNIT, "cores": threads, "kind": smp.kind,
+               "sample": f"{smp.desc}: {smp.name} ({smp.n} particles, 15 XPBI + 4 PBF iterations per "
+                         f"substep), {done} consecutive substeps in {dt:.1f} s on {threads} threads"}
 
 
 def host_threads() -> int:
@@ -177,27 +227,25 @@ def host_threads() -> int:
 
 
 def run_reference(args, rank: int, world: int):
+    """The reference's kernels on the host cores (rank 0 only), one substep
+    of the CPU sample per step, consecutive from the prerolled state."""
     if rank != 0:
         return
     threads = host_threads()
-    scale = args.cpu_scale
-    # warm-up + timed steps, each one substep of the bounded sample
+    smp = CpuSample(args.cpu_scale, args.preroll, threads)
     for _ in range(args.warmup):
-        cpu_baseline(scale, threads)
-    times, n, kind, desc = [], 0, "port", ""
-    for _ in range(args.steps):
-        v, n, dt, _, kind, desc = cpu_baseline(scale, threads)
-        times.append(dt)
-    total = sum(times)
-    value = n * args.steps / total
-    sample = (f"dam-breach scene scaled to {n} particles (z extent x{scale}), one substep "
-              f"(15 XPBI + 4 PBF iterations) per step from rest, {desc}, {threads} threads")
+        smp.step()
+    total = sum(smp.step() for _ in range(args.steps))
+    value = smp.n * args.steps / total
+    sample = (f"{smp.desc}: {smp.name} ({smp.n} particles), one substep (15 XPBI + 4 PBF iterations) "
+              f"per step, {threads} threads")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": args.workload, "solver": "plain", "cpu_sample_particles": n},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
+            "config": {"workload": args.workload, "solver": "plain", "cpu_sample": smp.name,
+                       "cpu_sample_particles": smp.n, "preroll_seconds": round(smp.preroll_s, 1)},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": smp.kind, "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -229,10 +277,20 @@ def max_over_ranks(x: float, dist, device: str = "cuda") -> float:
     return float(t.item())
 
 
-def job_throughput(particles_per_rank: int, world: int, steps: int, seconds: float) -> float:
+def job_particles(n_rank: int, dist, device: str = "cuda") -> int:
+    """Particles of the whole job: every rank's shard (all-reduce SUM)."""
+    if not dist:
+        return n_rank
+    import torch
+    t = torch.tensor([n_rank], dtype=torch.int64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return int(t.item())
+
+
+def job_throughput(job_particles_: int, steps: int, seconds: float) -> float:
     """Whole-job particle-substeps/s: every rank's particles over the slowest
-    rank's time (weak scaling: each rank steps its own scenes)."""
-    return particles_per_rank * world * steps / seconds
+    rank's time."""
+    return job_particles_ * steps / seconds
 
 
 def timed_steps(sim, has_water, steps, stream, dist):
@@ -261,12 +319,20 @@ def residual_stats(sim, has_water, n_scenes, substeps):
             r, u = sim.read_residuals(k)
             c = sim.read_contact_residuals(k)
             K = sim.scenes[k]["iterations"]
-            if r[0] > 0:
+            if r[0] > 0:  # a scene with constraints (its contact entry pairs with it; 0 with no contact)
                 rel.append(float(r[1 + K] / r[0]))
-            if c[0] > 0:
-                relc.append(float(c[1 + K] / c[0]))
+                relc.append(float(c[1 + K] / c[0]) if c[0] > 0 else 0.0)
             used.append(u)
     return rel, relc, used
+
+
+def reached_fraction(rel, relc, tau: float, tau_c: float) -> float:
+    """Fraction of tracked (scene, substep) solves whose final constraint AND
+    contact residuals (relative to their starting values) are both within
+    the plain solve's tolerances (0.01% slack for the f64 sums' rounding)."""
+    r = np.asarray(rel, np.float64)
+    c = np.asarray(relc, np.float64)
+    return float(np.mean((r <= tau * 1.0001) & (c <= tau_c * 1.0001))) if len(r) else 0.0
 
 
 def run_xpbi(args, rank: int, world: int):
@@ -277,8 +343,9 @@ def run_xpbi(args, rank: int, world: int):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    xp, scenes = workload(args.workload, rank)
-    n_total = sum(len(s["positions"]) for s in scenes)
+    xp, scenes, scaling = workload(args.workload, rank, world)
+    n_rank = sum(len(s["positions"]) for s in scenes)
+    n_job = job_particles(n_rank, dist)
     stream = torch.cuda.Stream()
     learned = args.solver == "learned"
 
@@ -292,7 +359,7 @@ def run_xpbi(args, rank: int, world: int):
     clocks.start()
     ms_plain = timed_steps(sim, has_water, args.steps, stream, dist)
     clk = clocks.stop()
-    value_plain = job_throughput(n_total, world, args.steps, ms_plain / 1e3)
+    value_plain = job_throughput(n_job, args.steps, ms_plain / 1e3)
     launches = sim.launches_per_substep(-1, has_water)
     solvers = {"plain": {"value": value_plain, "ms_per_step": ms_plain / args.steps,
                          "iterations": [s["iterations"] for s in scenes][:4]}}
@@ -318,7 +385,7 @@ def run_xpbi(args, rank: int, world: int):
         clocks.start()
         ms = timed_steps(sim, has_water, args.steps, stream, dist)
         clk = clocks.stop()
-        value = job_throughput(n_total, world, args.steps, ms / 1e3)
+        value = job_throughput(n_job, args.steps, ms / 1e3)
         launches = sim.launches_per_substep(-1, has_water)
         sim.set_solver(1, tau, True, False, contact_rel_tol=tau_c)
         rel_l, relc_l, used_l = residual_stats(sim, has_water, len(scenes), args.residual_substeps)
@@ -330,7 +397,7 @@ def run_xpbi(args, rank: int, world: int):
                               "final_rel_residual_median": float(np.median(rel_l)),
                               "final_rel_contact_residual_median": float(np.median(relc_l)) if relc_l else None,
                               "iterations_mean": float(np.mean(used_l)),
-                              "reached_tol_fraction": float(np.mean(np.array(rel_l) <= tau * 1.0001))}
+                              "reached_tol_fraction": reached_fraction(rel_l, relc_l, tau, tau_c)}
 
     # ---- end to end through the public API with host buffers: per step the
     # frame's writeParams from host memory, one substep, and the positions
@@ -353,11 +420,11 @@ def run_xpbi(args, rank: int, world: int):
     sim.synchronize()
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
-    e2e = job_throughput(n_total, world, args.steps, e2e_s)
+    e2e = job_throughput(n_job, args.steps, e2e_s)
     # uniforms uploaded per step: SceneDev (192 B) + MatDev table (8 x 48 B)
     # + packed material words (8 x 64 B) per scene
     h2d = len(scenes) * (192 + 8 * 48 + 8 * 64)
-    d2h = 16 * n_total
+    d2h = 16 * n_rank
 
     # ---- per-kernel times (events around each launch) for the roofline
     per = {}
@@ -379,14 +446,14 @@ def run_xpbi(args, rank: int, world: int):
     else:
         peak, peak_src = 6800.0, "fallback"
     n_water = sum(int(sum(1 for m in s["matIds"] if s["materials"][m]["kind"] == 6)) for s in scenes)
-    n_solid = n_total - n_water
+    n_solid = n_rank - n_water
     bs, bw = ALGO_BYTES.get(dom, (0, 0))
     algo = bs * n_solid + bw * n_water  # bytes per launch
     achieved = algo / (dom_avg_ms / 1e3) / 1e9
     tpp = NCU_TRAFFIC_PER_PARTICLE.get(dom)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_src,
-                "traffic": None if tpp is None else tpp * n_total,
+                "traffic": None if tpp is None else tpp * n_rank,
                 "traffic_source": "ncu capture of the 1M-particle dam breach scaled by particle count",
                 "algo_bytes_per_launch": algo, "solid_particles": n_solid, "water_particles": n_water,
                 "share": sum(per[dom]) / total_ms,
@@ -411,24 +478,23 @@ def run_xpbi(args, rank: int, world: int):
     sim.close()
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+           "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": scaling,
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": args.workload, "particles_per_gpu": n_total, "scenes": len(scenes),
+           "config": {"workload": args.workload, "particles_per_gpu": n_rank, "particles_job": n_job,
+                      "scenes": len(scenes),
                       "solver": args.solver, "preroll_substeps": args.preroll,
                       "iterations": [s["iterations"] for s in scenes][:4],
                       "autotuned_variants": {"solveA": tuned["solveA"], "solveB": tuned["solveB"],
                                              "solveA_ms": [round(x, 4) for x in tuned["solveA_ms"]],
                                              "solveB_ms": [round(x, 4) for x in tuned["solveB_ms"]]},
-                      "l2": "inputs larger than L2 (state ~1.3 GB per 4M particles)"},
+                      "l2": "inputs larger than L2 (state ~1.3 GB per 4M particles)",
+                      "cpu_sample": cpu_sample_name(args.cpu_scale, args.preroll)},
            "solvers": solvers,
            "roofline": roofline, "clocks": clk, "gpu_launches": launches * args.steps,
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}}
     if rank == 0 and not args.no_cpu_baseline:
-        v, n, dt, done, kind, desc = cpu_baseline(args.cpu_scale, host_threads(), substeps=args.cpu_substeps,
-                                                  budget_s=args.cpu_budget)
-        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": host_threads(), "kind": kind,
-                               "sample": f"{desc}, {done} dam-breach substeps (15 XPBI + 4 PBF iterations "
-                                         f"each) of {n} particles from rest, {dt:.1f} s"}
+        _, out["cpu_baseline"] = cpu_baseline(args.cpu_scale, args.preroll, host_threads(), args.cpu_substeps,
+                                              args.cpu_budget)
     if rank == 0:
         print(json.dumps(out))
     if dist:
@@ -458,7 +524,7 @@ def main():
     if args.solver is None:
         args.solver = "learned" if args.workload in ("dam_mix4", "dam_breach") else "plain"
     if args.preroll is None:
-        args.preroll = 100 if args.solver == "learned" else 0
+        args.preroll = 100 if (args.solver == "learned" or args.impl == "reference") else 0
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
     if args.impl == "reference":

@@ -114,3 +114,23 @@ def test_ppm_writer(xp, tmp_path):
     xp.render.write_ppm(str(tmp_path / "a.ppm"), img)
     data = (tmp_path / "a.ppm").read_bytes()
     assert data.startswith(b"P6\n3 2\n255\n") and data[len(b"P6\n3 2\n255\n") + 3:][:3] == bytes((10, 20, 30))
+
+
+def test_oracle_packing_equals_the_abi(xp, built_lib):
+    """The CPU paths pack their uniforms with oracle/uniforms.py (no library);
+    it must give the ABI's words for every demo scene and benchmark config,
+    including a collider and explicit damping."""
+    from oracle import uniforms as U
+    scenes = [f() for f in xp.scenes.SCENES.values()]
+    scenes += [xp.scenes.config_sand_column(), xp.scenes.config_nacc_snowball(),
+               xp.scenes.config_dam_breach(scale=0.05)]
+    scenes += xp.scenes.config_batch(n_scenes=12, seed=3)
+    for sc in scenes:
+        for over in ({}, dict(colliderActive=True, colliderPos=[0.1, 0.2, 0.3], colliderR=0.05,
+                              colliderVel=[1.0, -2.0, 0.5], time=0.25, kDamp=0.3)):
+            p = xp.params_for(sc, **over)
+            assert p == U.frame_params(sc, **over)
+            pw, mw = xp.pack_uniforms(sc, p)
+            opw, omw = U.pack(sc, p)
+            assert np.array_equal(pw, opw)
+            assert np.array_equal(mw, omw)

@@ -13,13 +13,23 @@ sys.path.insert(0, ROOT)
 
 def test_dam_mix_workloads_take_any_scene_count():
     import bench
-    _, two = bench.workload("dam_mix2")
-    assert len(two) == 2 and all(len(s["positions"]) == 1_000_000 for s in two)
-    _, two_r1 = bench.workload("dam_mix2", rank=1)  # rank 1 takes the next seeds
-    assert (two[0]["positions"] != two_r1[0]["positions"]).any()
+    _, two, scaling = bench.workload("dam_mix2")
+    assert len(two) == 2 and all(len(s["positions"]) == 1_000_000 for s in two) and scaling == "weak"
+    _, r0, _ = bench.workload("dam_mix2", rank=0, world=2)
+    _, r1, _ = bench.workload("dam_mix2", rank=1, world=2)  # the job's four seeds, two per rank
+    assert len(r0) == len(r1) == 2
+    seen = [s["positions"][:4].tobytes() for s in r0 + r1]
+    assert len(set(seen)) == 4
     for bad in ("dam_mix0", "dam_mix", "dam_mixx", "nope"):
         with pytest.raises(SystemExit):
             bench.workload(bad)
+
+
+def test_reached_fraction_needs_both_residuals():
+    import bench
+    assert bench.reached_fraction([1e-5, 1e-5], [0.01, 0.03], 2e-5, 0.02) == 0.5
+    assert bench.reached_fraction([3e-5, 1e-5], [0.01, 0.01], 2e-5, 0.02) == 0.5
+    assert bench.reached_fraction([1e-5], [0.0], 2e-5, 0.02) == 1.0
 
 
 def _line(t, sm, slowdown="Not Active", power_cap="Not Active"):

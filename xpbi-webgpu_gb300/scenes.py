@@ -7,7 +7,8 @@ workloads (sand column, NACC snowball, dam breach, a batch of 256 mixed
 scenes, and the 4-seed dam-breach mix).
 
 A scene is a dict with the fields ``new Simulation(device, scene)`` reads
-(sim.js:10-81) plus the frame-loop settings (main.js:385-402).
+(sim.js:10-81) plus the frame-loop settings (main.js:385-402). The module
+needs only NumPy, so CPU tools can load it without the library.
 """
 from __future__ import annotations
 
@@ -15,7 +16,8 @@ import math
 
 import numpy as np
 
-from ._abi import DP, ELASTIC, HB, NACC, SNOW, VM, WATER
+# material kinds, MAT of web/js/sim.js:4-7 (the ABI's XPBI_* kinds have the same values)
+ELASTIC, DP, NACC, VM, HB, SNOW, WATER = range(7)
 
 
 def _jsround(x: float) -> int:
