@@ -318,10 +318,9 @@ def residual_stats(sim, has_water, n_scenes, substeps):
         for k in range(n_scenes):
             r, u = sim.read_residuals(k)
             c = sim.read_contact_residuals(k)
-            K = sim.scenes[k]["iterations"]
             if r[0] > 0:  # a scene with constraints (its contact entry pairs with it; 0 with no contact)
-                rel.append(float(r[1 + K] / r[0]))
-                relc.append(float(c[1 + K] / c[0]) if c[0] > 0 else 0.0)
+                rel.append(float(r[-1] / r[0]))  # the final state's residual, re-measured over every particle
+                relc.append(float(c[-1] / c[0]) if c[0] > 0 else 0.0)
             used.append(u)
     return rel, relc, used
 
@@ -367,37 +366,76 @@ def run_xpbi(args, rank: int, world: int):
     if learned:
         # equal residual: the plain solve's own final constraint and contact
         # residuals, relative to their starting values, median over tracked
-        # substeps and scenes; the learned solve stops once both are reached
+        # substeps and scenes; the early-stopped solves stop once both are
+        # reached
         sim.set_solver(0, 0.0, True, True)
         rel, relc, _ = residual_stats(sim, has_water, len(scenes), args.residual_substeps)
         tau = float(np.median(rel))
         tau_c = float(np.median(relc)) if relc else 1.0
         sim.close()
-        tw = importlib.import_module("xpbi-webgpu_gb300.train_warm")
-        net = tw.load_weights()
-        sim, has_water = make_sim(xp, scenes, stream, args.preroll)
-        sim.set_variants(tuned["solveA"], tuned["solveB"])
-        sim.set_network(net)
-        sim.set_solver(1, tau, False, False, contact_rel_tol=tau_c)
-        sim.step(args.warmup, -1, has_water)
-        sim.synchronize()
-        clocks = Clocks(local)
-        clocks.start()
-        ms = timed_steps(sim, has_water, args.steps, stream, dist)
-        clk = clocks.stop()
-        value = job_throughput(n_job, args.steps, ms / 1e3)
-        launches = sim.launches_per_substep(-1, has_water)
-        sim.set_solver(1, tau, True, False, contact_rel_tol=tau_c)
-        rel_l, relc_l, used_l = residual_stats(sim, has_water, len(scenes), args.residual_substeps)
-        sim.set_solver(1, tau, False, False, contact_rel_tol=tau_c)
         solvers["plain"]["final_rel_residual_median"] = tau
         solvers["plain"]["final_rel_contact_residual_median"] = tau_c
-        solvers["learned"] = {"value": value, "ms_per_step": ms / args.steps, "rel_tol": tau,
-                              "contact_rel_tol": tau_c,
-                              "final_rel_residual_median": float(np.median(rel_l)),
-                              "final_rel_contact_residual_median": float(np.median(relc_l)) if relc_l else None,
-                              "iterations_mean": float(np.mean(used_l)),
-                              "reached_tol_fraction": reached_fraction(rel_l, relc_l, tau, tau_c)}
+        tw = importlib.import_module("xpbi-webgpu_gb300.train_warm")
+        net = tw.load_weights()
+        n_solid_rank = sum(int(sum(1 for m in s["matIds"] if s["materials"][m]["kind"] != 6)) for s in scenes)
+
+        def early_stopped(mode, share, keep=False):
+            """An early-stopped solve at the plain tolerances: mode 1 = the
+            network's warm start, 0 = the zero start; share > 0 = with the
+            active set. Returns (its solver record, the handle if keep)."""
+            h, _ = make_sim(xp, scenes, stream, args.preroll)
+            h.set_variants(tuned["solveA"], tuned["solveB"])
+            if mode == 1:
+                h.set_network(net)
+            h.set_active_set(share)
+            h.set_max_iterations(args.max_iterations)
+            h.set_solver(mode, tau, False, False, contact_rel_tol=tau_c)
+            h.step(args.warmup, -1, has_water)
+            h.synchronize()
+            ck = Clocks(local)
+            ck.start()
+            t = timed_steps(h, has_water, args.steps, stream, dist)
+            c = ck.stop()
+            h.set_solver(mode, tau, True, False, contact_rel_tol=tau_c)
+            rel_l, relc_l, used_l = residual_stats(h, has_water, len(scenes), args.residual_substeps)
+            act_a, act_b = h.read_active_counts()
+            h.set_solver(mode, tau, False, False, contact_rel_tol=tau_c)
+            rec = {"value": job_throughput(n_job, args.steps, t / 1e3), "ms_per_step": t / args.steps,
+                   "network": mode == 1, "active_share": share, "max_iterations": args.max_iterations,
+                   "rel_tol": tau, "contact_rel_tol": tau_c,
+                   "final_rel_residual_median": float(np.median(rel_l)),
+                   "final_rel_contact_residual_median": float(np.median(relc_l)) if relc_l else None,
+                   "iterations_mean": float(np.mean(used_l)),
+                   "reached_tol_fraction": reached_fraction(rel_l, relc_l, tau, tau_c)}
+            if share > 0:
+                K = max(max(s["iterations"] for s in scenes), args.max_iterations)
+                rec["active_fraction_per_iteration"] = {
+                    "solveA": [1.0] + [round(int(x) / max(n_solid_rank, 1), 4) for x in act_a[1:K]],
+                    "solveB": [1.0] + [round(int(x) / max(n_rank, 1), 4) for x in act_b[1:K]],
+                    "of": "solids (solveA), all particles (solveB); last tracked substep"}
+            return rec, (h, c) if keep else h.close()
+
+        solvers["learned"], (sim, clk) = early_stopped(1, args.active_share, keep=True)
+        value, ms = solvers["learned"]["value"], solvers["learned"]["ms_per_step"] * args.steps
+        launches = sim.launches_per_substep(-1, has_water)
+        if args.active_share > 0:
+            # the graph runs the iterations after the last PBF pass as a device
+            # loop: 6 launches (two compactions, solveA, solveB, the residual,
+            # the loop step) per iteration it runs plus one to start it, in
+            # place of the 5 per iteration up to the cap that an enqueued
+            # substep issues
+            pbf = [p_.get("pbfIterations", 0) or 0 for p_ in (xp.params_for(s_) for s_ in scenes)]
+            k0 = max(1, max(pbf))
+            cap = max(args.max_iterations, max(s_["iterations"] for s_ in scenes))
+            it = solvers["learned"]["iterations_mean"]
+            if cap - k0 >= 2:
+                launches = launches - 5 * (cap - k0) + 1 + 6 * max(0.0, it - k0)
+        if not args.no_ablation:
+            # what each part gains: the network without the active set, and
+            # the active set without the network (zero start)
+            if args.active_share > 0:
+                solvers["learned_without_active_set"], _ = early_stopped(1, 0.0)
+                solvers["plain_start_with_active_set"], _ = early_stopped(0, args.active_share)
 
     # ---- end to end through the public API with host buffers: per step the
     # frame's writeParams from host memory, one substep, and the positions
@@ -490,7 +528,7 @@ def run_xpbi(args, rank: int, world: int):
                       "l2": "inputs larger than L2 (state ~1.3 GB per 4M particles)",
                       "cpu_sample": cpu_sample_name(args.cpu_scale, args.preroll)},
            "solvers": solvers,
-           "roofline": roofline, "clocks": clk, "gpu_launches": launches * args.steps,
+           "roofline": roofline, "clocks": clk, "gpu_launches": int(round(launches * args.steps)),
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}}
     if rank == 0 and not args.no_cpu_baseline:
         _, out["cpu_baseline"] = cpu_baseline(args.cpu_scale, args.preroll, host_threads(), args.cpu_substeps,
@@ -519,6 +557,14 @@ def main():
                     help="learned warm start at the plain solve's residual (default for the dam-breach mix)")
     ap.add_argument("--preroll", type=int, default=None, help="untimed plain substeps before warm-up")
     ap.add_argument("--residual-substeps", type=int, default=4)
+    ap.add_argument("--active-share", type=float, default=0.25,
+                    help="active set of the learned solve: share of the residual budget settled particles may "
+                         "hold (0: no work skipping)")
+    ap.add_argument("--max-iterations", type=int, default=30,
+                    help="iteration cap of the early-stopped solves (they stop once both residuals reach the plain "
+                         "solve's; the plain solve runs its fixed 15)")
+    ap.add_argument("--no-ablation", action="store_true",
+                    help="skip the learned solve's ablation lines (network alone, active set alone)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.solver is None:

@@ -278,6 +278,41 @@ int xpbi_set_lanes(xpbi_sim* sim, int32_t lanes);
 int xpbi_set_solver(xpbi_sim* sim, int32_t mode, float rel_tol, float contact_rel_tol, int32_t track_residual,
                     int32_t log_features);
 
+/* Active set (no counterpart in the reference): work skipping for a solve
+ * with an early stop (rel_tol > 0, one lane per slot; ignored otherwise).
+ * Iteration 0 runs every particle. From iteration 1 on, a solid is
+ * re-evaluated only if its own velocity or a solid neighbour's moved since
+ * its last evaluation (otherwise its residuals are unchanged), takes an
+ * impulse only if its squared constraint residual exceeds share / nSolid of
+ * the scene's squared budget (rel_tol^2 times the iteration-0 sum), and
+ * applies a contact correction only above the same share of the contact
+ * budget; a particle's velocity is updated only if it was re-evaluated or a
+ * neighbour's impulse reaches it. A velocity change counts as a move if its
+ * square exceeds share * rel_tol^2 times the mean squared velocity change of
+ * iteration 0 (smaller ones shift a neighbour's residual by about its settle
+ * threshold or less). Settled particles hold about `share` of each budget,
+ * and the scene stops once the residual sums over all particles (the
+ * settled ones with their last values) are within tolerance; with
+ * track_residual the final state's residuals are re-measured over every
+ * particle. share = 0 turns it off (the default); 0 < share <= 1. */
+int xpbi_set_active_set(xpbi_sim* sim, float share);
+
+/* Iteration cap of an early-stopped solve (rel_tol > 0; no counterpart in
+ * the reference): each scene iterates until both of its residuals reach
+ * their tolerances or max_iterations iterations ran, whichever is first, so
+ * a solve that needs a few more iterations than the plain budget to reach
+ * the plain solve's residual still reaches it. PBF passes keep the scene's
+ * own schedule. 0 (the default) caps at the scene's own iteration count;
+ * at most 128. The residual histories then hold max(cap, iterations) + 2
+ * entries (the final state's residual last). */
+int xpbi_set_max_iterations(xpbi_sim* sim, int32_t max_iterations);
+
+/* Particles visited per iteration of the last substep, summed over scenes:
+ * solve_a[k] = solids solveA re-evaluated, solve_b[k] = particles solveB
+ * updated, for k >= 1 (iteration 0 visits every particle and records 0).
+ * Either pointer may be NULL; cap entries at most. */
+int xpbi_read_active_counts(xpbi_sim* sim, uint32_t* solve_a, uint32_t* solve_b, int32_t cap);
+
 /* Load the warm-start network's 9473 parameters (layout of xpbi_mlp_*).
  * Its output is alpha_tilde times the multiplier increment over the previous
  * substep's final multiplier. */
@@ -293,6 +328,15 @@ int xpbi_read_residuals(xpbi_sim* sim, uint32_t scene, double* norms, int32_t ca
  * xpbi_read_residuals: the norm of the contact position correction solveB
  * would apply at each iteration's velocities (norms[0] = iteration 0's). */
 int xpbi_read_contact_residuals(xpbi_sim* sim, uint32_t scene, double* norms, int32_t cap);
+
+/* Per-particle residuals of the last substep of one scene, in its cell
+ * order (the order of xpbi_read_state), squared: r2 = the constraint
+ * residual and c2 = the contact correction of the last pass that recorded
+ * them (with track_residual: the pass after the last iteration, i.e. of the
+ * final state), r0sq = the constraint residual at lambda = 0 entering
+ * iteration 0. Zeros for water and inactive constraints. Any pointer may be
+ * NULL. No counterpart in the reference. */
+int xpbi_read_particle_residuals(xpbi_sim* sim, uint32_t scene, float* r2, float* c2, float* r0sq);
 
 /* Training rows of the last substep of one scene (cell-sorted order):
  * features16 [n][16] (zeros for water; feature 4 is alpha_tilde times the

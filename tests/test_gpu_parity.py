@@ -180,6 +180,37 @@ def test_batched_scenes_match_single(xp, oracle, built_lib):
         compare(after[k], ref, ref64, has_pbf=sc["hasWater"])
 
 
+@pytest.mark.parametrize("lanes", [0, 4])
+def test_mixed_batch_sample_of_the_256_scene_config(xp, oracle, built_lib, lanes):
+    """Twenty scenes of the batched config's distribution (seed 3: every
+    plasticity model — Drucker-Prager, NACC, von Mises, Herschel-Bulkley,
+    snow — and 10 to 20 iterations per scene; 2k-8k particles each), one
+    handle, one launch per stage: after five substeps every scene's next
+    substep matches its own oracle run. lanes 0 is the library's choice for
+    this size (one lane per particle); 4 forces the small-scene path."""
+    scenes = xp.scenes.config_batch(n_scenes=20, seed=3, n_lo=2000, n_hi=8000)
+    kinds = {s["materials"][0]["kind"] for s in scenes}
+    its = [s["iterations"] for s in scenes]
+    assert kinds == {xp.scenes.DP, xp.scenes.NACC, xp.scenes.VM, xp.scenes.HB, xp.scenes.SNOW}
+    assert min(its) == 10 and max(its) == 20
+    with xp.Simulation(scenes) as sim:
+        sim.set_lanes(lanes)
+        for k, sc in enumerate(scenes):
+            sim.write_params(xp.params_for(sc), scene=k)
+            sim.set_schedule(k, sc["iterations"], sc["hasWater"])
+        sim.step(5, -1, False)
+        states = [sim.read_state(k) for k in range(len(scenes))]
+        uni = [sim.uniforms(k) for k in range(len(scenes))]
+        sim.encode_substep(-1, False)
+        after = [sim.read_state(k) for k in range(len(scenes))]
+    for k, sc in enumerate(scenes):
+        pw, mw = uni[k]
+        ref = oracle.substep(pw, mw, states[k], its[k], False, -1)
+        ref64 = oracle.substep(pw, mw, states[k], its[k], False, -1, f64=True)
+        compare(after[k], ref, ref64,
+                perturbed=perturbed_runs(oracle, sc, states[k], iterations=its[k], has_water=False, xp=xp))
+
+
 def test_profile_substep_labels(xp, built_lib):
     sc = xp.scenes.dam_breach()
     with xp.Simulation(sc) as sim:

@@ -220,6 +220,7 @@ void buildSceneDev(const SceneHost& s, uint32_t sceneIdx, SceneDev& d, MatDev* m
   d.dvCap = 0.2f * H / dt;
   d.iterations = s.iterations;
   d.pbfIterations = s.params.pbf_iterations;
+  d.pbfUntil = s.params.pbf_iterations < 0 ? s.iterations : std::min(s.iterations, s.params.pbf_iterations);
   d.hasWater = s.hasWater;
   for (int i = 0; i < kMaxMats; ++i) {
     const uint32_t* q = m + 16 * i;
@@ -285,6 +286,7 @@ struct xpbi_sim {
   // stream that waits for the work enqueued so far; a substep's position
   // update waits for the copies (an external event wait, also in graphs)
   cudaStream_t copy = nullptr;
+  cudaStream_t loop = nullptr;  // captures the body of the device loop (early-stopped solves in a graph)
   cudaEvent_t evWork = nullptr, evCopy = nullptr;
   bool copyPending = false;
   cudaGraph_t graph = nullptr;
@@ -296,6 +298,8 @@ struct xpbi_sim {
   float residTol = 0.f;     // early stop tolerance relative to |C(v_pred)|; <= 0 off
   float residTolC = 0.f;    // the contact residual's tolerance
   bool track = false;       // residual history per iteration
+  float activeShare = 0.f;  // active set: share of the residual budget settled slots may hold (0: off)
+  int maxIters = 0;         // an early-stopped solve may iterate up to this many times (0: the scene's count)
   bool features = false;    // compute network features every substep (training logs)
   bool netLoaded = false;
   float* netParams = nullptr;
@@ -337,6 +341,7 @@ void destroyAll(xpbi_sim* s) {
   if (s->own) cudaStreamDestroy(s->own);
   if (s->capture) cudaStreamDestroy(s->capture);
   if (s->copy) cudaStreamDestroy(s->copy);
+  if (s->loop) cudaStreamDestroy(s->loop);
   if (s->evWork) cudaEventDestroy(s->evWork);
   if (s->evCopy) cudaEventDestroy(s->evCopy);
 }
@@ -359,6 +364,12 @@ int upload(xpbi_sim* s) {
     buildSceneDev(s->sc[i], i, s->sdev[i], &s->mdev[(size_t)i * kMaxMats]);
     s->sdev[i].residTol = s->residTol;
     s->sdev[i].residTolC = s->residTolC;
+    s->sdev[i].asShare = s->activeShare;
+    if (s->residTol > 0.f && s->maxIters > s->sc[i].iterations) s->sdev[i].iterations = s->maxIters;
+    uint32_t solids = 0;
+    for (uint32_t m = 0; m < s->sc[i].nMats; ++m)
+      if (s->sc[i].mats[m].kind != XPBI_WATER) solids += s->sc[i].matCount[m];
+    s->sdev[i].nSolid = solids;
     for (uint32_t m = 0; m < s->sc[i].nMats; ++m)
       packMaterial(s->sc[i].mats[m], s->sc[i].V0, &s->matWordsHost[((size_t)i * kMaxMats + m) * XPBI_MATERIAL_WORDS]);
   }
@@ -369,6 +380,12 @@ int upload(xpbi_sim* s) {
                           s->stream));
   s->dirty = false;
   return XPBI_OK;
+}
+
+// Iterations a scene may run this substep: its own count, or for an
+// early-stopped solve the larger cap of xpbi_set_max_iterations.
+int effIterations(const xpbi_sim* s, const SceneHost& h) {
+  return s->residTol > 0.f && s->maxIters > h.iterations ? s->maxIters : h.iterations;
 }
 
 // The substep's launch schedule: max iterations and which iterations run PBF.
@@ -382,11 +399,13 @@ struct Schedule {
   bool keepLam = false;  // carry the final multipliers into the next substep
   int varA = 0, varB = 0; // solveA / solveB variants
   int lanes = 1;          // lanes per slot in solveA / solveB
+  bool active = false;    // active set (work skipping) in the iterations
   std::string key() const {
     std::string k = std::to_string(K) + ":";
     for (char c : pbf) k += c ? '1' : '0';
     k += ":" + std::to_string(mode) + (track ? "t" : "") + (reduce ? "r" : "") + (features ? "f" : "") +
-         (keepLam ? "l" : "") + ":v" + std::to_string(varA) + std::to_string(varB) + ":g" + std::to_string(lanes);
+         (keepLam ? "l" : "") + (active ? "a" : "") + ":v" + std::to_string(varA) + std::to_string(varB) + ":g" +
+         std::to_string(lanes);
     return k;
   }
 };
@@ -411,7 +430,9 @@ Schedule schedule(const xpbi_sim* s) {
         if (h.mats[m].kind != XPBI_WATER) solids += h.matCount[m];
     sch.lanes = solids <= kFourLaneSolids ? 4 : (solids <= kTwoLaneSolids ? 2 : 1);
   }
-  for (const SceneHost& h : s->sc) sch.K = std::max(sch.K, h.iterations);
+  // the active set needs the early stop's residual sums and one lane per slot
+  sch.active = s->activeShare > 0.f && s->residTol > 0.f && sch.lanes == 1;
+  for (const SceneHost& h : s->sc) sch.K = std::max(sch.K, effIterations(s, h));
   sch.pbf.assign(sch.K, 0);
   for (const SceneHost& h : s->sc) {
     if (!h.hasWater) continue;
@@ -435,10 +456,64 @@ struct Recorder {
   }
 };
 
+// One active-set iteration without a PBF pass (k may be kIterDevice): the
+// changed solids and the slots solveB updates compacted into lists, solveA
+// and solveB over them, the residual reduction.
+void enqueueListIteration(const Bufs& b, const Schedule& sch, int k, int aflags, cudaStream_t st, Recorder& R) {
+  const int act = kMarkMoved | kActive;
+  launch_compact(b, k, 0, st);
+  R.mark(st, "compact");
+  launch_solveA_list(b, k, b.velS[0], aflags | act, sch.varA, st);
+  R.mark(st, "solveA");
+  launch_compact(b, k, 1, st);
+  R.mark(st, "compact");
+  launch_solveB_list(b, k, b.velS[0], (sch.reduce ? kTrackResid : 0) | act, sch.varB, st);
+  R.mark(st, "solveB");
+  launch_resid_reduce(b, k, (aflags & kWarm) != 0, st);
+  R.mark(st, "residual");
+}
+
+// Inside a stream capture: the iterations k0..K-1 of an early-stopped
+// solve as a while node of the graph, whose body (one list iteration on the
+// device's iteration counter) repeats until every scene stopped or reached
+// its cap; no launch is spent on iterations nothing needs.
+cudaError_t captureDeviceLoop(xpbi_sim* s, const Schedule& sch, int k0, int aflags, cudaStream_t st) {
+  const Bufs& b = s->b;
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  cudaError_t e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd);
+  if (e != cudaSuccess) return e;
+  cudaGraphConditionalHandle h;
+  if ((e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
+  launch_loop_begin(b, k0, h, st);
+  if ((e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd)) != cudaSuccess) return e;
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  if ((e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &p)) != cudaSuccess) return e;
+  cudaGraph_t body = p.conditional.phGraph_out[0];
+  if ((e = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
+      cudaSuccess)
+    return e;
+  if ((e = cudaStreamBeginCaptureToGraph(s->loop, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed)) !=
+      cudaSuccess)
+    return e;
+  Recorder none;
+  enqueueListIteration(b, sch, kIterDevice, aflags, s->loop, none);
+  launch_loop_next(b, h, s->loop);
+  cudaGraph_t out = nullptr;
+  return cudaStreamEndCapture(s->loop, &out);
+}
+
 // encodeSubstep (sim.js:220-272). Ping-pong parity is resolved on the host:
 // the last writer's buffer is passed to updateF+integrate directly, so no
 // copy-back is needed (the reference copies velB -> velA when odd).
-void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder* rec) {
+cudaError_t enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder* rec) {
   const Bufs& b = s->b;
   Recorder none;
   Recorder& R = rec ? *rec : none;
@@ -472,32 +547,69 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
     cudaMemsetAsync(b.done, 0, sizeof(int) * b.S, st);
     cudaMemsetAsync(b.itersUsed, 0, sizeof(int) * b.S, st);
   }
+  if (sch.active) {  // nothing is marked before iteration 0, which visits every slot
+    const size_t padded = ((size_t)b.N + 15) & ~size_t(15);
+    cudaMemsetAsync(b.dirty[0], 0, padded, st);
+    cudaMemsetAsync(b.dirty[1], 0, padded, st);
+    cudaMemsetAsync(b.bmark, 0, padded, st);
+    cudaMemsetAsync(b.imp, 0, b.N, st);
+    cudaMemsetAsync(b.actA, 0, sizeof(uint32_t) * kMaxResid, st);
+    cudaMemsetAsync(b.actB, 0, sizeof(uint32_t) * kMaxResid, st);
+  }
   const int aflags = (sch.reduce ? kTrackResid : 0) | (sch.mode != 0 ? kWarm : 0);
   // solveA(k) records the scenes' largest solid displacement in slot k & 1
   // (the reorder cleared both), solveB(k) clears the other for iteration k+1
   int in = 0;
-  for (int k = 0; k < sch.K; ++k) {
+  // an early-stopped active-set solve captured into a graph runs its last
+  // iterations (from the first after which no PBF pass follows) as a device
+  // loop; elsewhere every iteration is enqueued (those past a scene's stop
+  // find nothing to do)
+  int kLoop = sch.K;
+  cudaStreamCaptureStatus capSt = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(st, &capSt);
+  if (sch.active && capSt == cudaStreamCaptureStatusActive) {
+    int k0 = sch.K;
+    while (k0 - 1 >= 1 && !sch.pbf[k0 - 1]) --k0;
+    if (sch.K - k0 >= 2) kLoop = k0;
+  }
+  for (int k = 0; k < kLoop; ++k) {
     // iteration 0 after a features pass: that pass already evaluated the
     // constraint at these velocities, with one lane per slot (several lanes
     // sum in another order, so they evaluate it again)
     const int stored = k == 0 && sch.features && sch.lanes == 1 ? kStoredC : 0;
-    launch_solveA(b, k, b.velS[in], aflags | stored, sch.varA, sch.lanes, st);
-    R.mark(st, "solveA");
-    launch_solveB(b, k, b.velS[in], b.velS[in ^ 1], sch.pbf[k] != 0, sch.reduce ? kTrackResid : 0, sch.varB,
-                  sch.lanes, st);
-    R.mark(st, "solveB");
+    // active set: iteration 0 visits every slot and marks what moved; later
+    // ones visit the marked slots; velocities update in place (solveB and
+    // pbfB read no neighbour's velocity), so there is no ping-pong
+    const int act = sch.active ? (kMarkMoved | (k > 0 ? kActive : 0)) : 0;
+    if (sch.active && k > 0 && !sch.pbf[k]) {
+      // no PBF pass follows: solveA and solveB run over compacted lists of
+      // the slots they visit (full warps however the slots are spread);
+      // velocities stay in velS[0] (in place from iteration 0 on)
+      enqueueListIteration(b, sch, k, aflags, st, R);
+      continue;
+    } else {
+      launch_solveA(b, k, b.velS[in], aflags | stored | (act & kActive), sch.varA, sch.lanes, st);
+      R.mark(st, "solveA");
+      launch_solveB(b, k, b.velS[in], b.velS[in ^ (sch.active ? 0 : 1)], sch.pbf[k] != 0,
+                    (sch.reduce ? kTrackResid : 0) | act, sch.varB, sch.lanes, st);
+      R.mark(st, "solveB");
+    }
     if (sch.reduce) {
       launch_resid_reduce(b, k, (aflags & kWarm) != 0, st);
       R.mark(st, "residual");
     }
-    in ^= 1;
+    if (!sch.active) in ^= 1;
     if (sch.pbf[k]) {
       launch_pbfA(b, k, b.velS[in], st);
       R.mark(st, "pbfA");
-      launch_pbfB(b, k, b.velS[in], b.velS[in ^ 1], st);
+      launch_pbfB(b, k, b.velS[in], b.velS[in ^ (sch.active ? 0 : 1)], sch.active ? kMarkMoved : 0, st);
       R.mark(st, "pbfB");
-      in ^= 1;
+      if (!sch.active) in ^= 1;
     }
+  }
+  if (kLoop < sch.K) {
+    const cudaError_t e = captureDeviceLoop(s, sch, kLoop, aflags, st);
+    if (e != cudaSuccess) return e;
   }
   if (sch.track) {  // residual of the state the iterations leave behind
     launch_solveA(b, sch.K, b.velS[in], kTrackResid | kMeasureOnly, sch.varA, sch.lanes, st);
@@ -524,11 +636,13 @@ void enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Recorder*
     launch_keep_lambda(b, st);
     R.mark(st, "keepLambda");
   }
+  return cudaSuccess;
 }
 
 int kernelsPerSubstep(const Schedule& sch) {
   int n = 5 /* count, scan, fill, bigcells, reorder */ + 1 /* computeL */ + 2 /* xsph, updateF+integrate */;
-  for (int k = 0; k < sch.K; ++k) n += 2 + (sch.pbf[k] ? 2 : 0) + (sch.reduce ? 1 : 0);
+  for (int k = 0; k < sch.K; ++k)
+    n += 2 + (sch.pbf[k] ? 2 : 0) + (sch.reduce ? 1 : 0) + (sch.active && k > 0 && !sch.pbf[k] ? 2 : 0);
   if (sch.features) n += 1;
   if (sch.mode == 1) n += 2;
   if (sch.mode == 2) n += 1;
@@ -572,6 +686,7 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   if (cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&s->capture, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&s->loop, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&s->evWork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&s->evCopy, cudaEventDisableTiming) != cudaSuccess)
     return bail(fail(XPBI_ERR_CUDA, "cudaStreamCreate failed"));
@@ -631,13 +746,25 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   A(b.c0sq, n);
   A(b.rc, n);
   A(b.solidDisp, 2 * (size_t)nScenes);
-  A(b.residPart, (size_t)nScenes * kResidChunks * 3);
+  A(b.residPart, (size_t)nScenes * kResidChunks * 4);
   A(b.residTicket, nScenes);
   A(b.resid, (size_t)nScenes * kMaxResid);
   A(b.residC, (size_t)nScenes * kMaxResid);
   A(b.c0, nScenes);
   A(b.cc0, nScenes);
   A(b.done, nScenes);
+  // flag arrays padded to whole 16-byte groups (the compaction reads 16 at once)
+  A(b.dirty[0], (n + 15) & ~size_t(15));
+  A(b.dirty[1], (n + 15) & ~size_t(15));
+  A(b.bmark, (n + 15) & ~size_t(15));
+  A(b.imp, n);
+  A(b.listA, n);
+  A(b.listB, n);
+  A(b.thr, 3 * (size_t)nScenes);
+  A(b.dv0sq, n);
+  A(b.actA, (size_t)kMaxResid);
+  A(b.actB, (size_t)kMaxResid);
+  A(b.kIter, 1);
   A(b.itersUsed, nScenes);
   {
     uint8_t* blob = nullptr;
@@ -686,6 +813,8 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
             cudaMemset(b.sortedIdx, 0, 4 * n) == cudaSuccess && cudaMemset(b.lamOut, 0, 4 * n) == cudaSuccess &&
             cudaMemset(b.lamPrev, 0, 4 * n) == cudaSuccess && cudaMemset(b.lamWarm, 0, 4 * n) == cudaSuccess &&
             cudaMemset(b.done, 0, sizeof(int) * nScenes) == cudaSuccess &&
+            cudaMemset(b.actA, 0, sizeof(uint32_t) * kMaxResid) == cudaSuccess &&
+            cudaMemset(b.actB, 0, sizeof(uint32_t) * kMaxResid) == cudaSuccess &&
             cudaMemset(b.itersUsed, 0, sizeof(int) * nScenes) == cudaSuccess &&
             cudaMemset(b.resid, 0, sizeof(double) * nScenes * kMaxResid) == cudaSuccess &&
             cudaMemset(b.residC, 0, sizeof(double) * nScenes * kMaxResid) == cudaSuccess &&
@@ -750,9 +879,15 @@ int ensureGraph(xpbi_sim* s, const Schedule& sch) {
     s->graph = nullptr;
   }
   XPBI_CK(cudaStreamBeginCapture(s->capture, cudaStreamCaptureModeThreadLocal));
-  enqueueSubstep(s, sch, s->capture, nullptr);
+  const cudaError_t qe = enqueueSubstep(s, sch, s->capture, nullptr);
   cudaGraph_t g = nullptr;
-  XPBI_CK(cudaStreamEndCapture(s->capture, &g));
+  const cudaError_t ee = cudaStreamEndCapture(s->capture, &g);  // ends the capture whatever happened
+  if (qe != cudaSuccess || ee != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return fail(XPBI_ERR_CUDA, std::string("substep graph capture: ") +
+                                   cudaGetErrorString(qe != cudaSuccess ? qe : ee));
+  }
   s->graph = g;
   XPBI_CK(cudaGraphInstantiate(&s->gexec, g, 0));
   s->gkey = key;
@@ -845,7 +980,7 @@ int xpbi_encode_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water) {
   XPBI_TRY(applySchedule(sim, iterations, has_water));
   XPBI_TRY(upload(sim));
   if (sim->b.N == 0) return XPBI_OK;
-  enqueueSubstep(sim, schedule(sim), sim->stream, nullptr);
+  XPBI_CK(enqueueSubstep(sim, schedule(sim), sim->stream, nullptr));
   XPBI_CK(cudaGetLastError());
   sim->fresh = false;
   sim->waterLPending = true;
@@ -1056,7 +1191,7 @@ int xpbi_profile_substep(xpbi_sim* sim, int32_t iterations, int32_t has_water, f
   Recorder rec;
   rec.ev = &ev;
   rec.labels = &lab;
-  enqueueSubstep(sim, schedule(sim), sim->stream, &rec);
+  XPBI_CK(enqueueSubstep(sim, schedule(sim), sim->stream, &rec));
   XPBI_CK(cudaGetLastError());
   XPBI_CK(cudaStreamSynchronize(sim->stream));
   sim->fresh = false;
@@ -1313,6 +1448,33 @@ int xpbi_set_solver(xpbi_sim* sim, int32_t mode, float rel_tol, float contact_re
   return XPBI_OK;
 }
 
+int xpbi_set_active_set(xpbi_sim* sim, float share) {
+  XPBI_TRY(checkSim(sim));
+  if (!(share >= 0.f && share <= 1.f)) return fail(XPBI_ERR_INVALID, "active-set share must be in [0, 1]");
+  sim->activeShare = share;
+  sim->dirty = true;
+  return XPBI_OK;
+}
+
+int xpbi_set_max_iterations(xpbi_sim* sim, int32_t max_iterations) {
+  XPBI_TRY(checkSim(sim));
+  if (max_iterations < 0 || max_iterations > kMaxResid - 1)
+    return fail(XPBI_ERR_INVALID, "max_iterations must be 0.." + std::to_string(kMaxResid - 1));
+  sim->maxIters = max_iterations;
+  sim->dirty = true;
+  return XPBI_OK;
+}
+
+int xpbi_read_active_counts(xpbi_sim* sim, uint32_t* solve_a, uint32_t* solve_b, int32_t cap) {
+  XPBI_TRY(checkSim(sim));
+  if (cap < 0) return fail(XPBI_ERR_INVALID, "cap must be >= 0");
+  XPBI_TRY(xpbi_synchronize(sim));
+  const int m = std::min<int>(cap, kMaxResid);
+  if (solve_a && m) XPBI_CK(cudaMemcpy(solve_a, sim->b.actA, sizeof(uint32_t) * m, cudaMemcpyDeviceToHost));
+  if (solve_b && m) XPBI_CK(cudaMemcpy(solve_b, sim->b.actB, sizeof(uint32_t) * m, cudaMemcpyDeviceToHost));
+  return XPBI_OK;
+}
+
 int xpbi_set_network(xpbi_sim* sim, const float* params, uint32_t count) {
   XPBI_TRY(checkSim(sim));
   if (!params || count != 9473u) return fail(XPBI_ERR_INVALID, "network needs 9473 parameters");
@@ -1335,7 +1497,7 @@ int xpbi_read_residuals(xpbi_sim* sim, uint32_t scene, double* norms, int32_t ca
                      cudaMemcpyDeviceToHost));
   XPBI_CK(cudaMemcpy(&c0, sim->b.c0 + scene, sizeof(double), cudaMemcpyDeviceToHost));
   XPBI_CK(cudaMemcpy(&used, sim->b.itersUsed + scene, sizeof(int), cudaMemcpyDeviceToHost));
-  const int K = sim->sc[scene].iterations;
+  const int K = effIterations(sim, sim->sc[scene]);
   if (iterations_run) *iterations_run = used;
   if (norms && cap > 0) {
     // [ |C(v_pred)|, |r_0| .. |r_{K-1}|, |r| after the last applied iteration ]
@@ -1359,7 +1521,7 @@ int xpbi_read_contact_residuals(xpbi_sim* sim, uint32_t scene, double* norms, in
                      cudaMemcpyDeviceToHost));
   XPBI_CK(cudaMemcpy(&c0, sim->b.cc0 + scene, sizeof(double), cudaMemcpyDeviceToHost));
   XPBI_CK(cudaMemcpy(&used, sim->b.itersUsed + scene, sizeof(int), cudaMemcpyDeviceToHost));
-  const int K = sim->sc[scene].iterations;
+  const int K = effIterations(sim, sim->sc[scene]);
   if (norms && cap > 0) {
     // same slots as xpbi_read_residuals; slot 0 repeats iteration 0's value
     std::vector<double> out;
@@ -1368,6 +1530,19 @@ int xpbi_read_contact_residuals(xpbi_sim* sim, uint32_t scene, double* norms, in
     out.push_back(std::sqrt(r[kMaxResid - 1]));
     for (int q = 0; q < cap && q < (int)out.size(); ++q) norms[q] = out[q];
   }
+  return XPBI_OK;
+}
+
+int xpbi_read_particle_residuals(xpbi_sim* sim, uint32_t scene, float* r2, float* c2, float* r0sq) {
+  XPBI_TRY(checkSim(sim));
+  if (scene >= sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
+  XPBI_TRY(xpbi_synchronize(sim));
+  const SceneHost& h = sim->sc[scene];
+  const size_t n = h.n, o = h.pBase;
+  if (n == 0) return XPBI_OK;
+  if (r2) XPBI_CK(cudaMemcpy(r2, sim->b.rr + o, sizeof(float) * n, cudaMemcpyDeviceToHost));
+  if (c2) XPBI_CK(cudaMemcpy(c2, sim->b.rc + o, sizeof(float) * n, cudaMemcpyDeviceToHost));
+  if (r0sq) XPBI_CK(cudaMemcpy(r0sq, sim->b.c0sq + o, sizeof(float) * n, cudaMemcpyDeviceToHost));
   return XPBI_OK;
 }
 

@@ -29,6 +29,8 @@
 // neighbour stencil never leaves the scene's own cells. Passes beyond a
 // scene's iteration budget copy velIn to velOut so the shared ping-pong
 // parity stays consistent for every scene.
+#include <algorithm>
+
 #include "xpbi_math.cuh"
 
 namespace xpbi {
@@ -594,6 +596,79 @@ __device__ __forceinline__ void recordSolidDisp(const Bufs& b, uint32_t i, int k
     atomicMax(b.solidDisp + (size_t)(k & 1) * b.S + sc, mx);
 }
 
+// ---------------------------------------------------------------- active set
+// The learned solve's work skipping (flags kActive / kMarkMoved, never set by
+// the reference solve). A slot's constraint depends on its own and its solid
+// neighbours' velocities, its contact correction on the predicted positions
+// of its solid neighbours: if none of those changed since the slot was last
+// evaluated, its residuals are unchanged too. So from iteration 1 on
+//   - solveA evaluates only the solids marked as changed (dirty); a solid
+//     whose residual is within the scene's per-slot threshold takes no
+//     impulse (its multiplier stays), the others update as the reference
+//     does and mark their solid neighbours (bmark) for solveB;
+//   - solveB visits only the changed or marked slots, updates velocities in
+//     place (it reads no neighbour's velocity), applies a contact correction
+//     only above the per-slot threshold, and a slot whose velocity changed
+//     by more than the scene's velocity scale marks itself and its solid
+//     neighbours as changed for the next iteration (as pbfB does);
+//   - residuals of slots not visited keep their last values, so the scene's
+//     residual sums and the early stop see every slot.
+// Iteration 0 runs every slot. The per-slot thresholds (formed once the
+// iteration-0 sums are known) give each settled slot an equal share of
+// asShare times the scene's residual budget, so settled slots alone can
+// never hold the scene above its tolerance. The velocity scale is the same
+// share of tol^2 times the mean squared velocity change of iteration 0: a
+// change below it moves a neighbour's residual by about that neighbour's
+// settle threshold or less, so the kept residuals are exact where nothing
+// moved and otherwise off by at most that much (a tracked solve re-measures
+// the final state over every slot).
+__device__ __forceinline__ void countWarp(uint32_t* ctr) {
+  const unsigned m = __activemask();
+  if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) atomicAdd(ctr, (uint32_t)__popc(m));
+}
+
+// flag[j] = 1 for every solid neighbour j of slot i (list order; the stencil
+// walk for an overflowed list). Plain byte stores: concurrent writers store
+// the same value.
+__device__ __forceinline__ void markSolidNbrs(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi,
+                                              uint8_t* __restrict__ flag) {
+  const uint32_t cnt = b.nbrCount[i];
+  if (cnt != kNbrOverflow) {
+    const uint4* __restrict__ L = reinterpret_cast<const uint4*>(listOf(b.nbr, i));
+    const uint32_t groups = (cnt + 3u) >> 2;
+#pragma unroll 1
+    for (uint32_t q = 0; q < groups; ++q) {
+      const uint4 g = __ldg(L + q);
+#pragma unroll
+      for (uint32_t t = 0; t < 4u; ++t) {
+        const uint32_t e = lane4(g, t);
+        if (4u * q + t < cnt && !(e & kWaterBit)) flag[e] = 1;
+      }
+    }
+  } else {
+    const SceneDev& S = *cx.scene;
+    forRows(S, b.cellStart, xi, [&](uint32_t beg, uint32_t end) {
+#pragma unroll 1
+      for (uint32_t j = beg; j < end; ++j) {
+        if (j == i) continue;
+        const float4 pj = ldg(b.posS + j);
+        const V3 d = xi - xyz(pj);
+        if (dot(d, d) < S.support2 && !waterW(pj.w)) flag[j] = 1;
+      }
+    });
+  }
+}
+
+__device__ __forceinline__ uint32_t sceneIndex(const Bufs& b, const Ctx& cx) {
+  return (uint32_t)(cx.scene - b.scenes);
+}
+
+// The iteration a launch works on: its argument, or inside the device loop
+// (argument kIterDevice) the loop's current iteration.
+__device__ __forceinline__ int iterK(const Bufs& b, int k) {
+  return k == kIterDevice ? *reinterpret_cast<volatile const int*>(b.kIter) : k;
+}
+
 // Inelastic constraint pass A (simkernels.js:248-309).
 //
 // flags & kTrackResid: writes r^2 for the residual of the state entering
@@ -625,7 +700,7 @@ __device__ __forceinline__ void recordSolidDisp(const Bufs& b, uint32_t i, int k
 template <bool kTrack>
 __device__ __forceinline__ void solveAUpdate(const Bufs& b, const Ctx& cx, uint32_t i, const float4& pi,
                                              const float4* __restrict__ velIn, uint32_t mi, const Constraint& c,
-                                             int k, bool warm0, bool measure) {
+                                             int k, bool warm0, bool measure, bool act = false) {
   const SceneDev& S = *cx.scene;
   constexpr bool track = kTrack;
   const float g = S.kDamp;
@@ -635,12 +710,14 @@ __device__ __forceinline__ void solveAUpdate(const Bufs& b, const Ctx& cx, uint3
   if (warm0 && !(fabsf(r0 + stiff * lam0) < fabsf(r0))) lam0 = 0.f;
   // the quantity the update drives to zero: r = C + alphaT lambda + gamma dt cdot
   const float lamTerm = warm0 ? stiff * lam0 : S.alphaT * lam0;
+  float r2 = 0.f;
   if (track) {
     // an inactive constraint (C below 1e-7: the reference skips the particle
     // and leaves its multiplier alone) has no residual; counting alphaT lambda
     // there would add a term no iteration can change
     const float r = c.C == 0.f ? 0.f : r0 + lamTerm;
-    b.rr[i] = r * r;
+    r2 = r * r;
+    b.rr[i] = r2;
     if (k == 0) b.c0sq[i] = r0 * r0;
   }
   // an inactive constraint still takes part in the contact pass
@@ -649,6 +726,12 @@ __device__ __forceinline__ void solveAUpdate(const Bufs& b, const Ctx& cx, uint3
   const float mass = cx.mats[mi].mass;
   if (measure) {  // the contact residual of these velocities, no impulse
     storeSp(b, i, mzero(), splat(0.f), xi, xci, mass);
+    return;
+  }
+  if (kTrack && act && (c.C == 0.f || r2 <= b.thr[3 * sceneIndex(b, cx)])) {
+    // settled (or inactive): no impulse (its stamp stays older than k + 1);
+    // solveB reads only the predicted position and mass of such a slot
+    b.Sp[3 * (size_t)b.N + i] = make_float4(xci.x, xci.y, xci.z, mass);
     return;
   }
   if (c.C == 0.f) {
@@ -660,6 +743,13 @@ __device__ __forceinline__ void solveAUpdate(const Bufs& b, const Ctx& cx, uint3
   b.lam[i] = lam0 + dlam;
   const float imp = warm0 ? lam0 + dlam : dlam;
   storeSp(b, i, mscale(c.GL, imp), c.sgrad * imp, xi, xci, mass);
+  if (kTrack && act) {
+    b.imp[i] = (uint8_t)(k + 1);
+    // its residual moves with its multiplier even where the velocity change
+    // rounds away: evaluate it again next iteration
+    b.dirty[(k + 1) & 1][i] = 1;
+    markSolidNbrs(b, cx, i, xi, b.bmark);  // their solveB applies this impulse
+  }
 }
 
 template <bool kTrack, int kMinB, int G, int kBlock = kThreads>
@@ -675,7 +765,12 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveA(Bufs b, int k, const f
   const bool warm0 = (flags & kWarm) != 0 && k == 0;
   const float4 pi = b.posS[i];
   const bool active = measure || (k < S.iterations && !sceneDone(b, i));
-  recordSolidDisp(b, i, k, active && !waterW(pi.w) && lane == 0 ? S.dt * length(xyz(velIn[i])) : 0.f);
+  // active set (one lane per slot): from iteration 1 a solid whose inputs
+  // did not change keeps its residual and takes no impulse
+  const bool act = kTrack && G == 1 && (flags & kActive) != 0 && k > 0;
+  bool changed = true;
+  if (act && active && !waterW(pi.w)) changed = b.dirty[k & 1][i] != 0;
+  recordSolidDisp(b, i, k, active && !waterW(pi.w) && lane == 0 && changed ? S.dt * length(xyz(velIn[i])) : 0.f);
   if (!active || waterW(pi.w)) {  // water: its record is never read
     if (track && lane == 0) {
       b.rr[i] = 0.f;
@@ -683,12 +778,91 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveA(Bufs b, int k, const f
     }
     return;
   }
+  if (act) {
+    if (!changed) return;
+    countWarp(b.actA + k);
+  }
   const uint32_t mi = matOfW(pi.w);
   const float st = b.stateS[i];
   const MatDev m = hardenedMat(cx.mats[mi], st);
   const Constraint c = evalConstraint<G>(b, cx, i, pi, velIn, m, st, lane);
   if (G > 1 && lane != 0) return;
-  solveAUpdate<kTrack>(b, cx, i, pi, velIn, mi, c, k, warm0, measure);
+  solveAUpdate<kTrack>(b, cx, i, pi, velIn, mi, c, k, warm0, measure, act);
+}
+
+// Active set, iterations without a PBF pass: the changed solid slots of the
+// scenes still iterating, appended to a list (warp-aggregated, in no
+// particular order: each slot's own sums keep their list order, so the
+// results do not depend on it); which = 1 lists the slots solveB updates
+// (changed or receiving an impulse). The list's length is the iteration's
+// visit count. Each thread reads the flags of 16 consecutive slots with one
+// 16-byte load per array (the flag arrays are padded to a multiple of 16),
+// checks the few flagged ones, and the warp appends its slots with one
+// atomic.
+constexpr int kCompactSlots = 16;
+__global__ void __launch_bounds__(kThreads) k_compact(Bufs b, int k, int which) {
+  k = iterK(b, k);
+  const uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) * kCompactSlots;
+  uint32_t take = 0;
+  if (base < b.N) {
+    uint4 f = *reinterpret_cast<const uint4*>(b.dirty[k & 1] + base);
+    if (which == 1) {
+      const uint4 m = *reinterpret_cast<const uint4*>(b.bmark + base);
+      f.x |= m.x; f.y |= m.y; f.z |= m.z; f.w |= m.w;
+    }
+    const uint32_t w[4] = {f.x, f.y, f.z, f.w};
+#pragma unroll
+    for (int q = 0; q < kCompactSlots; ++q) {
+      if (((w[q >> 2] >> (8 * (q & 3))) & 0xffu) == 0u) continue;
+      const uint32_t i = base + (uint32_t)q;
+      if (i >= b.N) break;
+      const uint32_t s = b.S > 1 ? (uint32_t)b.sceneOf[i] : 0u;
+      if (k < b.scenes[s].iterations && !b.done[s] && (which == 1 || !waterW(b.posS[i].w))) take |= 1u << q;
+    }
+  }
+  const uint32_t cnt = (uint32_t)__popc(take);
+  const unsigned lane = threadIdx.x & 31u;
+  uint32_t incl = cnt;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t n = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= (unsigned)off) incl += n;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  if (total == 0u) return;
+  uint32_t* ctr = which == 0 ? b.actA + k : b.actB + k;
+  uint32_t start = 0;
+  if (lane == 31u) start = atomicAdd(ctr, total);
+  start = __shfl_sync(0xffffffffu, start, 31) + incl - cnt;
+  uint32_t* out = which == 0 ? b.listA : b.listB;
+  while (take) {
+    const int q = __ffs(take) - 1;
+    take &= take - 1u;
+    out[start++] = base + (uint32_t)q;
+  }
+}
+
+// solveA over listA (iterations k >= 1 of the active set): the listed slots
+// with a grid-stride loop over a grid that fills the GPU once, so warps stay
+// full however the listed slots are spread.
+template <int kMinB, int kBlock>
+__global__ void __launch_bounds__(kBlock, kMinB) k_solveA_list(Bufs b, int k, const float4* __restrict__ velIn,
+                                                                int flags) {
+  k = iterK(b, k);
+  const uint32_t cnt = *(volatile const uint32_t*)(b.actA + k);
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < cnt; t += gridDim.x * blockDim.x) {
+    const uint32_t i = b.listA[t];
+    const Ctx cx = ctxOf(b, i);
+    const SceneDev& S = *cx.scene;
+    const float4 pi = b.posS[i];
+    recordSolidDisp(b, i, k, S.dt * length(xyz(velIn[i])));
+    const uint32_t mi = matOfW(pi.w);
+    const float st = b.stateS[i];
+    const MatDev m = hardenedMat(cx.mats[mi], st);
+    const Constraint c = evalConstraint<1>(b, cx, i, pi, velIn, m, st, 0);
+    solveAUpdate<true>(b, cx, i, pi, velIn, mi, c, k, false, false, true);
+  }
+  (void)flags;
 }
 
 // Iteration 0 after the features pass: the constraint that pass stored at
@@ -796,11 +970,12 @@ __global__ void k_warm_from_prev(Bufs b) {
 // which the constraint residual does not see). With a warm start, iteration
 // 0's constraint residual is the linearised estimate before the warm impulse
 // is applied, so it never stops the solve.
-constexpr int kResidSums = 3;
+constexpr int kResidSums = 4;
 constexpr int kResidWarps = 8;  // chunks per block, one warp each
 static_assert(kResidChunks % kResidWarps == 0, "whole blocks of chunks");
 __global__ void __launch_bounds__(32 * kResidWarps) k_resid(Bufs b, int k, int warm) {
   __shared__ bool lastBlock;
+  k = iterK(b, k);
   const uint32_t s = blockIdx.y;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t c = blockIdx.x * kResidWarps + (threadIdx.x >> 5);  // this warp's chunk
@@ -808,7 +983,8 @@ __global__ void __launch_bounds__(32 * kResidWarps) k_resid(Bufs b, int k, int w
   const uint32_t n = S.n, base = S.pBase;
   const uint32_t lo = base + (uint32_t)(((uint64_t)n * c) / kResidChunks);
   const uint32_t hi = base + (uint32_t)(((uint64_t)n * (c + 1)) / kResidChunks);
-  float a = 0.f, a0 = 0.f, ac = 0.f;
+  float a = 0.f, a0 = 0.f, ac = 0.f, av = 0.f;
+  const bool velSum = k == 0 && S.asShare > 0.f;  // the active set's velocity-change scale
   if (!b.done[s] || k < 0) {
     // the chunk's 16-byte-aligned interior as float4 (the arrays start on
     // 256-byte boundaries), its ragged ends (< 4 slots each) as scalars
@@ -817,11 +993,13 @@ __global__ void __launch_bounds__(32 * kResidWarps) k_resid(Bufs b, int k, int w
       a += b.rr[lo + lane];
       ac += b.rc[lo + lane];
       if (k == 0) a0 += b.c0sq[lo + lane];
+      if (velSum) av += b.dv0sq[lo + lane];
     }
     if (hi4 + lane < hi) {
       a += b.rr[hi4 + lane];
       ac += b.rc[hi4 + lane];
       if (k == 0) a0 += b.c0sq[hi4 + lane];
+      if (velSum) av += b.dv0sq[hi4 + lane];
     }
     const float4* __restrict__ rr4 = reinterpret_cast<const float4*>(b.rr);
     const float4* __restrict__ rc4 = reinterpret_cast<const float4*>(b.rc);
@@ -835,6 +1013,10 @@ __global__ void __launch_bounds__(32 * kResidWarps) k_resid(Bufs b, int k, int w
         const float4 z = c04[q];
         a0 += (z.x + z.y) + (z.z + z.w);
       }
+      if (velSum) {
+        const float4 z = reinterpret_cast<const float4*>(b.dv0sq)[q];
+        av += (z.x + z.y) + (z.z + z.w);
+      }
     }
   }
 #pragma unroll
@@ -842,12 +1024,14 @@ __global__ void __launch_bounds__(32 * kResidWarps) k_resid(Bufs b, int k, int w
     a += __shfl_xor_sync(0xffffffffu, a, off);
     a0 += __shfl_xor_sync(0xffffffffu, a0, off);
     ac += __shfl_xor_sync(0xffffffffu, ac, off);
+    av += __shfl_xor_sync(0xffffffffu, av, off);
   }
   if (lane == 0) {
     double* part = b.residPart + (s * kResidChunks + c) * kResidSums;
     part[0] = (double)a;
     part[1] = (double)a0;
     part[2] = (double)ac;
+    part[3] = (double)av;
     __threadfence();  // the partials are visible before this block's ticket
   }
   __syncthreads();
@@ -863,18 +1047,20 @@ __global__ void __launch_bounds__(32 * kResidWarps) k_resid(Bufs b, int k, int w
   __threadfence();
   if (lane == 0) b.residTicket[s] = 0u;  // every block of this launch has taken its ticket
   if (k >= 0 && (b.done[s] || k >= S.iterations)) return;
-  double ta = 0.0, ta0 = 0.0, tac = 0.0;
+  double ta = 0.0, ta0 = 0.0, tac = 0.0, tav = 0.0;
   for (int q = (int)lane; q < kResidChunks; q += 32) {
     const double* part = b.residPart + (s * kResidChunks + q) * kResidSums;
     ta += __ldcg(part);
     ta0 += __ldcg(part + 1);
     tac += __ldcg(part + 2);
+    tav += __ldcg(part + 3);
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
     ta += __shfl_xor_sync(0xffffffffu, ta, off);
     ta0 += __shfl_xor_sync(0xffffffffu, ta0, off);
     tac += __shfl_xor_sync(0xffffffffu, tac, off);
+    tav += __shfl_xor_sync(0xffffffffu, tav, off);
   }
   if (lane != 0) return;
   if (k < 0) {
@@ -886,11 +1072,20 @@ __global__ void __launch_bounds__(32 * kResidWarps) k_resid(Bufs b, int k, int w
     b.resid[(size_t)s * kMaxResid + k] = ta;
     b.residC[(size_t)s * kMaxResid + k] = tac;
   }
+  const double tol = (double)S.residTol, tolC = (double)S.residTolC;
   if (k == 0) {
     b.c0[s] = ta0;
     b.cc0[s] = tac;
+    // active set: a settled slot may hold up to asShare / nSolid of the
+    // scene's squared residual budget (tol^2 of the iteration-0 sums)
+    const double share = (double)S.asShare / (double)max(S.nSolid, 1u);
+    b.thr[3 * s] = (float)(share * tol * tol * ta0);
+    b.thr[3 * s + 1] = (float)(share * tolC * tolC * tac);
+    // a velocity change at the scale the converged solve still makes (the
+    // tolerance times iteration 0's) moves a neighbour's residual by about
+    // its own settle threshold: smaller ones do not count as moved
+    b.thr[3 * s + 2] = (float)(share * tol * tol * tav);
   }
-  const double tol = (double)S.residTol, tolC = (double)S.residTolC;
   if (tol > 0.0 && ta <= tol * tol * b.c0[s] && tac <= tolC * tolC * b.cc0[s] && !(warm && k == 0)) b.done[s] = 1;
   b.itersUsed[s] = k + 1;
 }
@@ -1085,8 +1280,187 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveB(Bufs b, int k, const f
   }
 }
 
+// solveB under the active set (one lane per slot; the launch passes
+// velOut == velIn: a slot reads only its own velocity, so the update is in
+// place and slots not visited keep theirs without a copy). flags & kActive
+// (iterations >= 1): only slots marked as changed (dirty) or receiving a
+// neighbour's impulse (bmark) run; a changed slot re-evaluates its contact
+// correction and applies it only above the scene's per-slot threshold, a
+// slot that only receives impulses keeps its (unchanged, unapplied)
+// contact correction. A neighbour's impulse record is gathered only if it
+// took an impulse (imp); its predicted position and mass (the record's
+// fourth plane) are current for every solid. flags & kMarkMoved: a slot
+// whose velocity changed marks itself and its solid neighbours as changed
+// for iteration k + 1. The scene's solid displacement bound carries into
+// the next iteration's slot (solveA raises it for the slots it visits).
+// One slot of solveB under the active set; `listed`: the slot came from
+// listB (changed or marked), so the flags are only cleared.
+__device__ __forceinline__ void solveBActiveSlot(const Bufs& b, int k, float4* __restrict__ vel, int writeXc,
+                                                 int flags, uint32_t i, bool listed) {
+  const Ctx cx = ctxOf(b, i);
+  const SceneDev& S = *cx.scene;
+  const float4 pi = b.posS[i];
+  if (k >= S.iterations || sceneDone(b, i)) {
+    if (writeXc) {
+      const float4 vi4 = vel[i];
+      const V3 xc = xyz(pi) + S.dt * xyz(vi4);
+      b.xc[i] = make_float4(xc.x, xc.y, xc.z, pi.w);
+    }
+    return;
+  }
+  const bool skip = (flags & kActive) != 0 && k > 0;
+  bool changed = true;
+  if (skip) {
+    uint8_t* __restrict__ dk = b.dirty[k & 1];
+    changed = dk[i] != 0;
+    const bool marked = b.bmark[i] != 0;
+    if (changed) dk[i] = 0;
+    if (marked) b.bmark[i] = 0;
+    if (!changed && !marked) {
+      if (writeXc) {
+        const float4 vi4 = vel[i];
+        const V3 xc = xyz(pi) + S.dt * xyz(vi4);
+        b.xc[i] = make_float4(xc.x, xc.y, xc.z, pi.w);
+      }
+      return;
+    }
+    if (!listed) countWarp(b.actB + k);
+  }
+  const uint8_t stamp = (uint8_t)(k + 1);
+  const float4 vi4 = vel[i];
+  const uint32_t mi = matOfW(pi.w);
+  const MatDev& m = cx.mats[mi];
+  const V3 xi = xyz(pi);
+  const bool iWater = waterW(pi.w);
+  V3 dv = splat(0.f), corr = splat(0.f);
+  if (!iWater) {
+    const size_t N = b.N;
+    const float4* __restrict__ Sp = b.Sp;
+    if (!skip || b.imp[i] == stamp) dv = xyz(b.SpSelf[i]);
+    const float Vi = vi4.w;
+    const V3 xci = xi + S.dt * xyz(vi4);
+    const float minD = S.minD;
+    const float massI = m.mass;
+    const float reach = (minD + S.dt * length(xyz(vi4)) +
+                         __uint_as_float(__ldg(b.solidDisp + (size_t)(k & 1) * b.S + sceneIndex(b, cx)))) *
+                        1.01f;
+    const float reach2 = reach * reach;
+    auto contact = [&](const float4& r3) {
+      const V3 dxc = xci - xyz(r3);
+      const float d2 = dot(dxc, dxc);
+      if (d2 < minD * minD && d2 > 1e-18f) {
+        const float rinv = rsqrtf(d2);
+        const float dist = d2 * rinv;
+        const float mb = r3.w;
+        const float w = mb / (massI + mb);
+        corr = corr + dxc * (rinv * ((minD - dist) * w));
+      }
+    };
+    auto visit = [&](uint32_t j) {
+      const bool jImp = !skip || b.imp[j] == stamp;
+      if (jImp) {
+        const float4* R = Sp + j;
+        const float4 r0 = ldg(R), r1 = ldg(R + N), r2 = ldg(R + 2 * N);
+        const V3 pb = v3(r0.w, r1.w, r2.w);
+        const M3 Sb = {{xyz(r0), xyz(r1), xyz(r2)}};
+        const V3 dxp = pb - xi;
+        dv = dv + Vi * mul(Sb, gradWFast(S, dxp));
+        if (changed && dot(dxp, dxp) < reach2) contact(ldg(Sp + 3 * N + j));
+      } else if (changed) {
+        contact(ldg(Sp + 3 * N + j));
+      }
+    };
+    const uint32_t cnt = b.nbrCount[i];
+    if (cnt != kNbrOverflow) {
+      const uint4* __restrict__ L = reinterpret_cast<const uint4*>(listOf(b.nbr, i));
+      const uint32_t groups = (cnt + 3u) >> 2;
+#pragma unroll 1
+      for (uint32_t q = 0; q < groups; ++q) {
+        const uint4 g = __ldg(L + q);
+#pragma unroll
+        for (uint32_t t = 0; t < 4u; ++t) {
+          const uint32_t e = lane4(g, t);
+          if (4u * q + t < cnt && !(e & kWaterBit)) visit(e);
+        }
+      }
+    } else {
+      forRows(S, b.cellStart, xi, [&](uint32_t beg, uint32_t end) {
+#pragma unroll 1
+        for (uint32_t j = beg; j < end; ++j) {
+          if (j == i) continue;
+          const float4 pj = ldg(b.posS + j);
+          const V3 d = xi - xyz(pj);
+          if (dot(d, d) < S.support2 && !waterW(pj.w)) visit(j);
+        }
+      });
+    }
+    if (changed) {
+      const float c2 = dot(corr, corr);
+      b.rc[i] = c2;
+      if (skip && c2 <= b.thr[3 * sceneIndex(b, cx) + 1]) corr = splat(0.f);  // settled: left unapplied
+    } else {
+      corr = splat(0.f);  // unchanged since last evaluated: at or below the threshold, not applied
+    }
+  } else if (changed) {
+    b.rc[i] = 0.f;
+  }
+  V3 dvv = dv / (m.mass * S.dt);
+  const float dvl = length(dvv);
+  if (dvl > S.dvCap) dvv = dvv * (S.dvCap / dvl);
+  V3 v = xyz(vi4) + dvv + corr * (S.contactOmega / S.dt);
+  v = applyBoundary(S, xi + S.dt * v, v, xi, m.boundFriction);
+  vel[i] = make_float4(v.x, v.y, v.z, vi4.w);
+  if (writeXc) {
+    const V3 xc = xi + S.dt * v;
+    b.xc[i] = make_float4(xc.x, xc.y, xc.z, pi.w);
+  }
+  const V3 dvel = v - xyz(vi4);
+  const float dv2 = dot(dvel, dvel);
+  if (k == 0) b.dv0sq[i] = iWater ? 0.f : dv2;
+  // moved: any change in iteration 0; later, a change above the scene's scale
+  if ((flags & kMarkMoved) && (k == 0 ? (v.x != vi4.x || v.y != vi4.y || v.z != vi4.z)
+                                      : dv2 > b.thr[3 * sceneIndex(b, cx) + 2])) {
+    uint8_t* __restrict__ dn = b.dirty[(k + 1) & 1];
+    dn[i] = 1;
+    if (!iWater) markSolidNbrs(b, cx, i, xi, dn);
+  }
+}
+
+// solveB under the active set (one lane per slot; the launch passes one
+// velocity array: a slot reads only its own velocity, so the update is in
+// place and slots not visited keep theirs without a copy). flags & kActive
+// (iterations >= 1): only slots marked as changed (dirty) or receiving a
+// neighbour's impulse (bmark) run; a changed slot re-evaluates its contact
+// correction and applies it only above the scene's per-slot threshold, a
+// slot that only receives impulses keeps its (unchanged, unapplied)
+// contact correction. A neighbour's impulse record is gathered only if it
+// took an impulse this iteration (its stamp is k + 1); its predicted
+// position and mass (the record's fourth plane) are current for every
+// solid. flags & kMarkMoved: a slot whose velocity changed (after iteration
+// 0: by more than the scene's velocity scale) marks itself and its solid
+// neighbours as changed for iteration k + 1. The scene's solid displacement
+// bound carries into the next iteration's slot (solveA raises it for the
+// slots it visits). With `list` the launch runs over listB (grid-stride),
+// else one thread per slot.
+template <int kMinB, int kBlock = kThreads>
+__global__ void __launch_bounds__(kBlock, kMinB) k_solveB_active(Bufs b, int k, float4* __restrict__ vel, int writeXc,
+                                                                 int flags, int list) {
+  k = iterK(b, k);
+  const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint32_t q = t0; q < b.S; q += gridDim.x * blockDim.x)  // carried into the next iteration's slot
+    b.solidDisp[(size_t)((k + 1) & 1) * b.S + q] = b.solidDisp[(size_t)(k & 1) * b.S + q];
+  if (list) {
+    const uint32_t cnt = *(volatile const uint32_t*)(b.actB + k);
+    for (uint32_t t = t0; t < cnt; t += gridDim.x * blockDim.x)
+      solveBActiveSlot(b, k, vel, writeXc, flags, b.listB[t], true);
+    return;
+  }
+  const uint32_t i = (gridDim.x - 1u - blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < b.N) solveBActiveSlot(b, k, vel, writeXc, flags, i, false);
+}
+
 __device__ __forceinline__ bool pbfActive(const SceneDev& S, int k) {
-  return S.hasWater && k < S.iterations && (S.pbfIterations < 0 || k < S.pbfIterations);
+  return S.hasWater && k < S.pbfUntil;
 }
 
 // ---------------------------------------------------------------- pbfA
@@ -1192,8 +1566,7 @@ struct PBData {
 // ---------------------------------------------------------------- pbfB
 // PBF position correction with s_corr (simkernels.js:441-477) over pbfA's
 // record of predicted neighbours.
-__global__ void XPBI_LB_PBF k_pbfB(Bufs b, int k, const float4* __restrict__ velIn,
-                                                    float4* __restrict__ velOut) {
+__global__ void XPBI_LB_PBF k_pbfB(Bufs b, int k, const float4* velIn, float4* velOut, int flags) {
   // blocks run last to first: the pass starts where pbfA ended, on
   // slots whose data is still in L2
   const uint32_t i = (gridDim.x - 1u - blockIdx.x) * blockDim.x + threadIdx.x;
@@ -1252,6 +1625,16 @@ __global__ void XPBI_LB_PBF k_pbfB(Bufs b, int k, const float4* __restrict__ vel
   const float scale = iWater ? 1.f : 0.5f;
   const V3 v = xyz(vi4) + dp * (scale / S.dt);
   velOut[i] = make_float4(v.x, v.y, v.z, vi4.w);
+  // active set: the next iteration revisits a slot this pass moved (and a
+  // moved solid's solid neighbours, whose constraint and contact inputs it is)
+  if (flags & kMarkMoved) {
+    const V3 dvel = v - xyz(vi4);
+    if (dot(dvel, dvel) > b.thr[3 * (uint32_t)(cx.scene - b.scenes) + 2]) {
+      uint8_t* __restrict__ dn = b.dirty[(k + 1) & 1];
+      dn[i] = 1;
+      if (!iWater) markSolidNbrs(b, cx, i, xyz(pi), dn);
+    }
+  }
 }
 
 // ---------------------------------------------------------------- xsph
@@ -1317,6 +1700,31 @@ __global__ void XPBI_LB_UPDATE k_updateF_integrate(Bufs b, const float4* __restr
   V3 x = xyz(pi) + S.dt * v;
   x = v3(clampf(x.x, S.dmin[0], S.dmax[0]), clampf(x.y, S.dmin[1], S.dmax[1]), clampf(x.z, S.dmin[2], S.dmax[2]));
   b.pos[i] = make_float4(x.x, x.y, x.z, fabsf(pi.w));
+}
+
+// ---------------------------------------------------------------- device loop
+// Whether any scene still iterates at iteration k: not stopped by its
+// residuals and below its iteration cap (one block; every thread returns it).
+__device__ __forceinline__ bool anyIterating(const Bufs& b, int k) {
+  bool run = false;
+  for (uint32_t s = threadIdx.x; s < b.S; s += blockDim.x)
+    run |= !b.done[s] && k < b.scenes[s].iterations;
+  return __syncthreads_or(run) != 0;
+}
+__global__ void k_loop_begin(Bufs b, int k0, cudaGraphConditionalHandle h) {
+  const bool run = anyIterating(b, k0);
+  if (threadIdx.x == 0) {
+    *b.kIter = k0;
+    cudaGraphSetConditional(h, run ? 1u : 0u);
+  }
+}
+__global__ void k_loop_next(Bufs b, cudaGraphConditionalHandle h) {
+  const int k = *reinterpret_cast<volatile const int*>(b.kIter) + 1;
+  const bool run = anyIterating(b, k);  // its barrier orders every read of kIter before the write
+  if (threadIdx.x == 0) {
+    *b.kIter = k;
+    cudaGraphSetConditional(h, run ? 1u : 0u);
+  }
 }
 
 inline unsigned grid(uint32_t n) { return (unsigned)((n + kThreads - 1) / kThreads); }
@@ -1387,9 +1795,41 @@ void solveBVariant(const Bufs& b, int k, const float4* velIn, float4* velOut, in
   k_solveB<kSolveBMinB[V], 1, kSolveBBlock[V]><<<gridOf(b.N, kSolveBBlock[V]), kSolveBBlock[V], 0, st>>>(
       b, k, velIn, velOut, wx, flags);
 }
+// A grid that fills the GPU once with this kernel's resident blocks (the
+// list launches loop over their lists).
+inline unsigned fillGrid(const void* fn, int block) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, 0);
+  return (unsigned)(std::max(1, sms) * std::max(1, per));
+}
+template <int V>
+void solveBActiveVariant(const Bufs& b, int k, float4* vel, int wx, int flags, bool list, cudaStream_t st) {
+  auto fn = k_solveB_active<kSolveBMinB[V], kSolveBBlock[V]>;
+  const unsigned g = list ? fillGrid((const void*)fn, kSolveBBlock[V]) : gridOf(b.N, kSolveBBlock[V]);
+  fn<<<g, kSolveBBlock[V], 0, st>>>(b, k, vel, wx, flags, list ? 1 : 0);
+}
+template <int V>
+void solveAListVariant(const Bufs& b, int k, const float4* velIn, int flags, cudaStream_t st) {
+  constexpr int minB = kSolveAMinB[V];
+  auto fn = k_solveA_list<minB, kSolveABlock[V]>;
+  fn<<<fillGrid((const void*)fn, kSolveABlock[V]), kSolveABlock[V], 0, st>>>(b, k, velIn, flags);
+}
 void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, int flags, int variant,
                    int lanes, cudaStream_t st) {
   const int wx = writeXc ? 1 : 0;
+  if (flags & (kActive | kMarkMoved)) {  // the active set: in place, one lane per slot
+    float4* vel = velOut;
+    switch (variant) {
+      case 1: solveBActiveVariant<1>(b, k, vel, wx, flags, false, st); break;
+      case 2: solveBActiveVariant<2>(b, k, vel, wx, flags, false, st); break;
+      case 3: solveBActiveVariant<3>(b, k, vel, wx, flags, false, st); break;
+      case 4: solveBActiveVariant<4>(b, k, vel, wx, flags, false, st); break;
+      default: solveBActiveVariant<0>(b, k, vel, wx, flags, false, st); break;
+    }
+    return;
+  }
   if (lanes == 4) {
     k_solveB<0, 4><<<grid(4u * b.N), kThreads, 0, st>>>(b, k, velIn, velOut, wx, flags);
     return;
@@ -1406,12 +1846,40 @@ void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bo
     default: solveBVariant<0>(b, k, velIn, velOut, wx, flags, st); break;
   }
 }
+void launch_loop_begin(const Bufs& b, int k0, cudaGraphConditionalHandle h, cudaStream_t st) {
+  k_loop_begin<<<1, 256, 0, st>>>(b, k0, h);
+}
+void launch_loop_next(const Bufs& b, cudaGraphConditionalHandle h, cudaStream_t st) {
+  k_loop_next<<<1, 256, 0, st>>>(b, h);
+}
+void launch_compact(const Bufs& b, int k, int which, cudaStream_t st) {
+  k_compact<<<grid((b.N + kCompactSlots - 1) / kCompactSlots), kThreads, 0, st>>>(b, k, which);
+}
+void launch_solveA_list(const Bufs& b, int k, const float4* velIn, int flags, int variant, cudaStream_t st) {
+  switch (variant) {
+    case 1: solveAListVariant<1>(b, k, velIn, flags, st); break;
+    case 2: solveAListVariant<2>(b, k, velIn, flags, st); break;
+    case 3: solveAListVariant<3>(b, k, velIn, flags, st); break;
+    case 4: solveAListVariant<4>(b, k, velIn, flags, st); break;
+    case 5: solveAListVariant<5>(b, k, velIn, flags, st); break;
+    default: solveAListVariant<0>(b, k, velIn, flags, st); break;
+  }
+}
+void launch_solveB_list(const Bufs& b, int k, float4* vel, int flags, int variant, cudaStream_t st) {
+  switch (variant) {
+    case 1: solveBActiveVariant<1>(b, k, vel, 0, flags, true, st); break;
+    case 2: solveBActiveVariant<2>(b, k, vel, 0, flags, true, st); break;
+    case 3: solveBActiveVariant<3>(b, k, vel, 0, flags, true, st); break;
+    case 4: solveBActiveVariant<4>(b, k, vel, 0, flags, true, st); break;
+    default: solveBActiveVariant<0>(b, k, vel, 0, flags, true, st); break;
+  }
+}
 void launch_pbfA(const Bufs& b, int k, const float4* velIn, cudaStream_t st) {
   (void)velIn;  // predicted positions were stored by the preceding solveB
   k_pbfA<<<grid(b.N), kThreads, 0, st>>>(b, k);
 }
-void launch_pbfB(const Bufs& b, int k, const float4* velIn, float4* velOut, cudaStream_t st) {
-  k_pbfB<<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut);
+void launch_pbfB(const Bufs& b, int k, const float4* velIn, float4* velOut, int flags, cudaStream_t st) {
+  k_pbfB<<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, flags);
 }
 void launch_xsph(const Bufs& b, const float4* velIn, float4* velOut, cudaStream_t st) {
   k_xsph<<<grid(b.N), kThreads, 0, st>>>(b, velIn, velOut);

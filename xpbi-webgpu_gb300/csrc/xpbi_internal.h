@@ -27,6 +27,11 @@ constexpr int kTrackResid = 1;         // write per-particle residuals
 constexpr int kWarm = 2;               // iteration 0 starts from lamWarm
 constexpr int kMeasureOnly = 4;        // residual only: no multiplier / impulse update
 constexpr int kStoredC = 8;            // iteration 0 reads the constraint the features pass stored
+// active set (solveA / solveB / pbfB flags)
+constexpr int kMarkMoved = 16;         // a slot whose velocity changed marks itself (and, if solid, its solid
+                                       // neighbours) as changed for the next iteration
+constexpr int kActive = 32;            // iteration k >= 1 visits only the slots whose inputs changed
+constexpr int kIterDevice = -1000000;  // a kernel's iteration argument: read it from Bufs::kIter (device loop)
 constexpr uint32_t kNbrOverflow = 0xffffffffu;
 constexpr uint32_t kWaterBit = 0x80000000u;
 
@@ -68,12 +73,15 @@ struct SceneDev {
   float dvCap;              // 0.2 support / dt            simkernels.js:361
   float invH;               // 1 / h
   float invW0;              // 1 / max(w0, 1e-12)          simkernels.js:466
-  int iterations;           // XPBI Jacobi iterations this substep
+  int iterations;           // XPBI Jacobi iterations this substep (an early-stopped solve's cap)
   int pbfIterations;        // PBF passes (first k iterations)
+  int pbfUntil;             // iterations k < pbfUntil run a PBF pass (the scene's own schedule)
   int hasWater;
   float residTol;           // early stop at |r_k| <= residTol |C(v_pred)|; <= 0: never
   float residTolC;          // ... and |contact_k| <= residTolC |contact_0|
   float waterMpd;           // mass / density of the scene's one water material; 0: none or several
+  uint32_t nSolid;          // solid particles of the scene
+  float asShare;            // active set: share of the residual budget settled particles may hold (0: off)
 };
 
 struct MatDev {
@@ -132,13 +140,26 @@ struct Bufs {
   float* c0sq;          // [N] squared constraint value at the predicted velocities
   float* rc;            // [N] squared contact correction of the current iteration
   uint32_t* solidDisp;  // [2][S] float bits: largest dt |v| of a scene's solids entering iteration k (slot k & 1)
-  double* residPart;    // [S][kResidChunks][3] partial sums
+  double* residPart;    // [S][kResidChunks][4] partial sums
   uint32_t* residTicket; // [S] blocks of the residual reduction done (0 between launches)
   double* resid;        // [S][kMaxResid] residual norm^2 per iteration (last slot: after the last)
   double* residC;       // [S][kMaxResid] contact residual norm^2, same slots
   double* c0;           // [S] |C(v_pred)|^2
   double* cc0;          // [S] contact residual^2 entering iteration 0
   int* done;            // [S] converged: later iterations skip
+  // active set: per-slot flags (bytes, set by plain stores of 1 from any thread)
+  uint8_t* dirty[2];    // [N] by iteration parity: the slot's constraint or contact inputs changed
+  uint8_t* bmark;       // [N] a solid neighbour received an impulse in this iteration's solveA
+  uint8_t* imp;         // [N] k + 1 if the slot took an impulse in iteration k (solveB gathers its record only
+                        //   then); cleared each substep
+  uint32_t* listA;      // [N] solid slots solveA re-evaluates this iteration (compacted)
+  uint32_t* listB;      // [N] slots solveB updates this iteration (compacted)
+  float* thr;           // [S][3] squared per-slot thresholds: settled constraint, settled contact, and the
+                        //   velocity change below which a slot does not count as moved
+  float* dv0sq;         // [N] |velocity change|^2 of each solid in iteration 0 (its scale for the last one)
+  uint32_t* actA;       // [kMaxResid] solid slots solveA evaluated, per iteration (listA's length)
+  uint32_t* actB;       // [kMaxResid] slots solveB updated, per iteration (listB's length)
+  int* kIter;           // [1] iteration of the device loop's current pass (kIterDevice)
   int* itersUsed;       // [S] iterations whose update was applied
   void* netBlob;        // packed network weights
   SceneDev* scenes;     // [S]
@@ -178,7 +199,19 @@ cudaError_t mlp_forward(const float* dX, uint32_t rows, const void* dBlob, float
 void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, int flags, int variant,
                    int lanes, cudaStream_t st);
 void launch_pbfA(const Bufs& b, int k, const float4* velIn, cudaStream_t st);
-void launch_pbfB(const Bufs& b, int k, const float4* velIn, float4* velOut, cudaStream_t st);
+// active set, iterations without a PBF pass: compact the changed solids
+// (which = 0, listA) or the changed and impulse-receiving slots (which = 1,
+// listB), then run solveA / solveB over the list
+void launch_compact(const Bufs& b, int k, int which, cudaStream_t st);
+void launch_solveA_list(const Bufs& b, int k, const float4* velIn, int flags, int variant, cudaStream_t st);
+void launch_solveB_list(const Bufs& b, int k, float4* vel, int flags, int variant, cudaStream_t st);
+// the device loop over an early-stopped solve's last iterations (a while
+// node of the substep's graph): begin sets the iteration to k0, next
+// advances it; both set the node's condition to whether any scene is still
+// iterating (not stopped, below its cap)
+void launch_loop_begin(const Bufs& b, int k0, cudaGraphConditionalHandle h, cudaStream_t st);
+void launch_loop_next(const Bufs& b, cudaGraphConditionalHandle h, cudaStream_t st);
+void launch_pbfB(const Bufs& b, int k, const float4* velIn, float4* velOut, int flags, cudaStream_t st);
 void launch_xsph(const Bufs& b, const float4* velIn, float4* velOut, cudaStream_t st);
 void launch_updateF_integrate(const Bufs& b, const float4* velIn, cudaStream_t st);
 

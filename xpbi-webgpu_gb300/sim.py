@@ -23,6 +23,13 @@ def _uptr(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_uint32))
 
 
+def _written(out):
+    """The entries a residual read-back filled (the buffer starts at -1, a
+    value no norm takes; skipped iterations are NaN)."""
+    filled = np.flatnonzero(~(out == -1.0))
+    return out[: filled[-1] + 1] if len(filled) else out[:0]
+
+
 def make_materials(materials) -> C.Array:
     arr = (Material * max(1, len(materials)))()
     for k, m in enumerate(materials):
@@ -267,15 +274,14 @@ class Simulation:
 
     def read_residuals(self, scene: int = 0):
         """(norms, iterations run): norms[0] = |C(v_pred)|, norms[1+k] =
-        |r_k|, norms[-1] = residual of the final state."""
-        it = self.scenes[scene]["iterations"] if "iterations" in self.scenes[scene] else 0
-        cap = 256
-        out = np.full(cap, np.nan)
+        |r_k| (NaN after an early stop), norms[-1] = residual of the final
+        state (with track_residual). The length is the scene's iteration
+        count (or an early-stopped solve's cap) + 2."""
+        out = np.full(256, -1.0)
         used = C.c_int32()
-        check(lib().xpbi_read_residuals(self._h, scene, out.ctypes.data_as(C.POINTER(C.c_double)), cap,
+        check(lib().xpbi_read_residuals(self._h, scene, out.ctypes.data_as(C.POINTER(C.c_double)), 256,
                                         C.byref(used)))
-        del it
-        return out, used.value
+        return _written(out), used.value
 
     SOLVEA_VARIANTS, SOLVEB_VARIANTS = 6, 5
 
@@ -297,9 +303,13 @@ class Simulation:
 
     def read_contact_residuals(self, scene: int = 0):
         """Contact residual norms in the slots of read_residuals."""
-        out = np.full(256, np.nan)
+        out = np.full(256, -1.0)
         check(lib().xpbi_read_contact_residuals(self._h, scene, out.ctypes.data_as(C.POINTER(C.c_double)), 256))
-        return out
+        return _written(out)
+
+    def set_max_iterations(self, max_iterations: int):
+        """Iteration cap of an early-stopped solve (0: the scene's count)."""
+        check(lib().xpbi_set_max_iterations(self._h, int(max_iterations)))
 
     def read_training(self, scene: int = 0):
         n = self.scene_sizes[scene]
@@ -308,6 +318,28 @@ class Simulation:
         a = np.zeros(1, np.float32)
         check(lib().xpbi_read_training(self._h, scene, _fptr(f), _fptr(t), _fptr(a)))
         return f, t, float(a[0])
+
+    def set_active_set(self, share: float):
+        """Work skipping in an early-stopped solve (0 turns it off); see
+        xpbi_set_active_set."""
+        check(lib().xpbi_set_active_set(self._h, float(share)))
+
+    def read_active_counts(self, cap: int = 129):
+        """(solveA re-evaluations, solveB updates) per iteration of the last
+        substep, summed over scenes (iteration 0 visits everything: 0)."""
+        a = np.zeros(cap, np.uint32)
+        b = np.zeros(cap, np.uint32)
+        check(lib().xpbi_read_active_counts(self._h, _uptr(a), _uptr(b), cap))
+        return a, b
+
+    def read_particle_residuals(self, scene: int = 0):
+        """(r2, c2, r0sq) per particle of the last substep (cell order):
+        squared constraint residual and contact correction of the last
+        recording pass, squared constraint residual at lambda = 0."""
+        n = self.scene_sizes[scene]
+        r2, c2, r0 = (np.empty(n, np.float32) for _ in range(3))
+        check(lib().xpbi_read_particle_residuals(self._h, scene, _fptr(r2), _fptr(c2), _fptr(r0)))
+        return r2, c2, r0
 
     def device_ptrs(self):
         p, v, m = C.c_void_p(), C.c_void_p(), C.c_void_p()
