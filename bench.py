@@ -313,16 +313,31 @@ def residual_stats(sim, has_water, n_scenes, substeps):
     values, and iterations applied, over `substeps` tracked substeps of every
     scene."""
     rel, relc, used = [], [], []
+    sim.fallbacks = []
     for _ in range(substeps):
         sim.step(1, -1, has_water)
         for k in range(n_scenes):
             r, u = sim.read_residuals(k)
             c = sim.read_contact_residuals(k)
+            sim.fallbacks.append(sim.read_fallback(k))
             if r[0] > 0:  # a scene with constraints (its contact entry pairs with it; 0 with no contact)
                 rel.append(float(r[-1] / r[0]))  # the final state's residual, re-measured over every particle
                 relc.append(float(c[-1] / c[0]) if c[0] > 0 else 0.0)
             used.append(u)
     return rel, relc, used
+
+
+def profile_kernels(sim, has_water, substeps: int) -> dict:
+    """Per-launch times (CUDA events around each launch) of `substeps`
+    enqueued substeps: label -> list of milliseconds."""
+    per = {}
+    for _ in range(max(1, substeps)):
+        for line in sim.profile_substep(-1, has_water).splitlines():
+            if ":" not in line:
+                continue
+            name, t = line.rsplit(":", 1)
+            per.setdefault(name.strip(), []).append(float(t.strip().replace("ms", "")))
+    return per
 
 
 def reached_fraction(rel, relc, tau: float, tau_c: float) -> float:
@@ -358,6 +373,7 @@ def run_xpbi(args, rank: int, world: int):
     clocks.start()
     ms_plain = timed_steps(sim, has_water, args.steps, stream, dist)
     clk = clocks.stop()
+    per_plain = profile_kernels(sim, has_water, args.profile_substeps)
     value_plain = job_throughput(n_job, args.steps, ms_plain / 1e3)
     launches = sim.launches_per_substep(-1, has_water)
     solvers = {"plain": {"value": value_plain, "ms_per_step": ms_plain / args.steps,
@@ -406,7 +422,8 @@ def run_xpbi(args, rank: int, world: int):
                    "final_rel_residual_median": float(np.median(rel_l)),
                    "final_rel_contact_residual_median": float(np.median(relc_l)) if relc_l else None,
                    "iterations_mean": float(np.mean(used_l)),
-                   "reached_tol_fraction": reached_fraction(rel_l, relc_l, tau, tau_c)}
+                   "reached_tol_fraction": reached_fraction(rel_l, relc_l, tau, tau_c),
+                   "resolved_plainly_fraction": float(np.mean(h.fallbacks)) if h.fallbacks else 0.0}
             if share > 0:
                 K = max(max(s["iterations"] for s in scenes), args.max_iterations)
                 rec["active_fraction_per_iteration"] = {
@@ -459,20 +476,19 @@ def run_xpbi(args, rank: int, world: int):
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
     e2e = job_throughput(n_job, args.steps, e2e_s)
-    # uniforms uploaded per step: SceneDev (192 B) + MatDev table (8 x 48 B)
+    # uniforms uploaded per step: SceneDev (244 B) + MatDev table (8 x 48 B)
     # + packed material words (8 x 64 B) per scene
-    h2d = len(scenes) * (192 + 8 * 48 + 8 * 64)
+    h2d = len(scenes) * (244 + 8 * 48 + 8 * 64)
     d2h = 16 * n_rank
 
-    # ---- per-kernel times (events around each launch) for the roofline
-    per = {}
-    for _ in range(max(1, args.profile_substeps)):
-        prof = sim.profile_substep(-1, has_water)
-        for line in prof.splitlines():
-            if ":" not in line:
-                continue
-            name, t = line.rsplit(":", 1)
-            per.setdefault(name.strip(), []).append(float(t.strip().replace("ms", "")))
+    # ---- per-kernel times (events around each launch) for the roofline: of
+    # the plain solve (every kernel over every particle); the learned
+    # solve's time per kernel and substep is reported beside it
+    per = per_plain
+    if learned:
+        per_l = profile_kernels(sim, has_water, args.profile_substeps)
+        reps = max(1, args.profile_substeps)
+        solvers["learned"]["substep_ms_by_kernel"] = {k: round(sum(v) / reps, 4) for k, v in per_l.items()}
     total_ms = sum(sum(v) for v in per.values())
     dom = max(per, key=lambda k: sum(per[k]))
     dom_avg_ms = statistics.mean(per[dom])

@@ -307,6 +307,17 @@ int xpbi_set_active_set(xpbi_sim* sim, float share);
  * entries (the final state's residual last). */
 int xpbi_set_max_iterations(xpbi_sim* sim, int32_t max_iterations);
 
+/* The judge of an early-stopped solve that differs from the reference (a
+ * warm start, or the active set; no counterpart in the reference): a scene
+ * whose constraint or contact residual has not reached its tolerance when
+ * its iteration cap runs out is re-solved in the same substep with the
+ * reference solve (lambda from 0, its own iteration count and PBF passes)
+ * from the velocities that entered iteration 0, and keeps that result.
+ * *resolved = 1 if scene `scene` was re-solved in the last substep. In a
+ * graph the re-solve sits behind a conditional node, so it costs nothing
+ * when every scene stopped. */
+int xpbi_read_fallback(xpbi_sim* sim, uint32_t scene, int32_t* resolved);
+
 /* Particles visited per iteration of the last substep, summed over scenes:
  * solve_a[k] = solids solveA re-evaluated, solve_b[k] = particles solveB
  * updated, for k >= 1 (iteration 0 visits every particle and records 0).

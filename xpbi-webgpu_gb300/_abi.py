@@ -33,6 +33,7 @@ EXPORTS = (
     "xpbi_render", "xpbi_set_lanes", "xpbi_read_positions_async", "xpbi_test_wait_expiry",
     "xpbi_sort_cells_noalloc_status", "xpbi_test_noalloc_wait_expiry", "xpbi_read_particle_residuals",
     "xpbi_set_active_set", "xpbi_read_active_counts", "xpbi_set_max_iterations",
+    "xpbi_read_fallback",
 )
 
 
@@ -112,6 +113,7 @@ _SIGS = {
     "xpbi_read_particle_residuals": (C.c_int, [_P, C.c_uint32, _F32P, _F32P, _F32P]),
     "xpbi_set_active_set": (C.c_int, [_P, C.c_float]),
     "xpbi_set_max_iterations": (C.c_int, [_P, C.c_int32]),
+    "xpbi_read_fallback": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_int32)]),
     "xpbi_read_active_counts": (C.c_int, [_P, _U32P, _U32P, C.c_int32]),
     "xpbi_read_contact_residuals": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_double), C.c_int32]),
     "xpbi_autotune": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32), _F32P, C.c_int32]),

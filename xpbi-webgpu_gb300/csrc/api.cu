@@ -221,6 +221,7 @@ void buildSceneDev(const SceneHost& s, uint32_t sceneIdx, SceneDev& d, MatDev* m
   d.iterations = s.iterations;
   d.pbfIterations = s.params.pbf_iterations;
   d.pbfUntil = s.params.pbf_iterations < 0 ? s.iterations : std::min(s.iterations, s.params.pbf_iterations);
+  d.plainIterations = s.iterations;
   d.hasWater = s.hasWater;
   for (int i = 0; i < kMaxMats; ++i) {
     const uint32_t* q = m + 16 * i;
@@ -400,11 +401,12 @@ struct Schedule {
   int varA = 0, varB = 0; // solveA / solveB variants
   int lanes = 1;          // lanes per slot in solveA / solveB
   bool active = false;    // active set (work skipping) in the iterations
+  bool fallback = false;  // scenes an early-stopped solve fails are re-solved plainly
   std::string key() const {
     std::string k = std::to_string(K) + ":";
     for (char c : pbf) k += c ? '1' : '0';
     k += ":" + std::to_string(mode) + (track ? "t" : "") + (reduce ? "r" : "") + (features ? "f" : "") +
-         (keepLam ? "l" : "") + (active ? "a" : "") + ":v" + std::to_string(varA) + std::to_string(varB) + ":g" +
+         (keepLam ? "l" : "") + (active ? "a" : "") + (fallback ? "j" : "") + ":v" + std::to_string(varA) + std::to_string(varB) + ":g" +
          std::to_string(lanes);
     return k;
   }
@@ -432,6 +434,9 @@ Schedule schedule(const xpbi_sim* s) {
   }
   // the active set needs the early stop's residual sums and one lane per slot
   sch.active = s->activeShare > 0.f && s->residTol > 0.f && sch.lanes == 1;
+  // an early-stopped solve that differs from the reference (a warm start or
+  // the active set) is judged against the plain tolerances it was given
+  sch.fallback = s->residTol > 0.f && (s->mode != 0 || sch.active);
   for (const SceneHost& h : s->sc) sch.K = std::max(sch.K, effIterations(s, h));
   sch.pbf.assign(sch.K, 0);
   for (const SceneHost& h : s->sc) {
@@ -510,6 +515,74 @@ cudaError_t captureDeviceLoop(xpbi_sim* s, const Schedule& sch, int k0, int afla
   return cudaStreamEndCapture(s->loop, &out);
 }
 
+// The plain re-solve of the scenes the judge marked: their velocities back
+// to vel0, then the reference schedule (lambda from 0, every slot of those
+// scenes, the scenes' own iteration counts and PBF passes) with the other
+// scenes' velocities copied through the ping-pong; the result ends in
+// velS[in] like the solve it replaces.
+void enqueuePlainResolve(xpbi_sim* s, const Schedule& sch, int in, cudaStream_t st, Recorder& R) {
+  const Bufs& b = s->b;
+  launch_restore(b, b.velS[in], st);
+  R.mark(st, "restore");
+  int cur = in;
+  int K = 0;
+  for (const SceneHost& h : s->sc) K = std::max(K, h.iterations);
+  for (int k = 0; k < K; ++k) {
+    const bool pbf = k < (int)sch.pbf.size() && sch.pbf[k];
+    launch_solveA(b, k, b.velS[cur], kRerun, sch.varA, sch.lanes, st);
+    R.mark(st, "solveA");
+    launch_solveB(b, k, b.velS[cur], b.velS[cur ^ 1], pbf, kRerun, sch.varB, sch.lanes, st);
+    R.mark(st, "solveB");
+    cur ^= 1;
+    if (pbf) {
+      launch_pbfA(b, k, b.velS[cur], kRerun, st);
+      R.mark(st, "pbfA");
+      launch_pbfB(b, k, b.velS[cur], b.velS[cur ^ 1], kRerun, st);
+      R.mark(st, "pbfB");
+      cur ^= 1;
+    }
+  }
+  if (cur != in) {
+    launch_copy_vel(b, b.velS[cur], b.velS[in], st);
+    R.mark(st, "copy");
+  }
+}
+
+// Inside a stream capture: the judge, then the plain re-solve as the body
+// of a conditional node the judge's kernel switches on only when a scene
+// failed.
+cudaError_t captureFallback(xpbi_sim* s, const Schedule& sch, int in, cudaStream_t st) {
+  const Bufs& b = s->b;
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  cudaError_t e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd);
+  if (e != cudaSuccess) return e;
+  cudaGraphConditionalHandle h;
+  if ((e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
+  launch_judge(b, h, true, st);
+  if ((e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd)) != cudaSuccess) return e;
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeIf;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  if ((e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &p)) != cudaSuccess) return e;
+  cudaGraph_t body = p.conditional.phGraph_out[0];
+  if ((e = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
+      cudaSuccess)
+    return e;
+  if ((e = cudaStreamBeginCaptureToGraph(s->loop, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed)) !=
+      cudaSuccess)
+    return e;
+  Recorder none;
+  enqueuePlainResolve(s, sch, in, s->loop, none);
+  cudaGraph_t out = nullptr;
+  return cudaStreamEndCapture(s->loop, &out);
+}
+
 // encodeSubstep (sim.js:220-272). Ping-pong parity is resolved on the host:
 // the last writer's buffer is passed to updateF+integrate directly, so no
 // copy-back is needed (the reference copies velB -> velA when odd).
@@ -557,6 +630,8 @@ cudaError_t enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Re
     cudaMemsetAsync(b.actB, 0, sizeof(uint32_t) * kMaxResid, st);
   }
   const int aflags = (sch.reduce ? kTrackResid : 0) | (sch.mode != 0 ? kWarm : 0);
+  if (sch.fallback)  // the plain re-solve starts from these velocities
+    cudaMemcpyAsync(b.vel0, b.velS[0], sizeof(float4) * (size_t)b.N, cudaMemcpyDeviceToDevice, st);
   // solveA(k) records the scenes' largest solid displacement in slot k & 1
   // (the reorder cleared both), solveB(k) clears the other for iteration k+1
   int in = 0;
@@ -600,7 +675,7 @@ cudaError_t enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Re
     }
     if (!sch.active) in ^= 1;
     if (sch.pbf[k]) {
-      launch_pbfA(b, k, b.velS[in], st);
+      launch_pbfA(b, k, b.velS[in], 0, st);
       R.mark(st, "pbfA");
       launch_pbfB(b, k, b.velS[in], b.velS[in ^ (sch.active ? 0 : 1)], sch.active ? kMarkMoved : 0, st);
       R.mark(st, "pbfB");
@@ -610,6 +685,19 @@ cudaError_t enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Re
   if (kLoop < sch.K) {
     const cudaError_t e = captureDeviceLoop(s, sch, kLoop, aflags, st);
     if (e != cudaSuccess) return e;
+  }
+  if (sch.fallback) {
+    // the judge: scenes that did not stop within their cap are re-solved
+    // with the reference solve from vel0 (in a graph, behind a conditional
+    // node that skips the body when every scene stopped)
+    if (capSt == cudaStreamCaptureStatusActive) {
+      const cudaError_t e = captureFallback(s, sch, in, st);
+      if (e != cudaSuccess) return e;
+    } else {
+      launch_judge(b, 0, false, st);
+      R.mark(st, "judge");
+      enqueuePlainResolve(s, sch, in, st, R);
+    }
   }
   if (sch.track) {  // residual of the state the iterations leave behind
     launch_solveA(b, sch.K, b.velS[in], kTrackResid | kMeasureOnly, sch.varA, sch.lanes, st);
@@ -648,6 +736,7 @@ int kernelsPerSubstep(const Schedule& sch) {
   if (sch.mode == 2) n += 1;
   if (sch.track) n += 3;
   if (sch.keepLam) n += 1;
+  if (sch.fallback) n += 1;  // the judge (its plain re-solve launches only when a scene failed)
   return n;
 }
 
@@ -765,6 +854,8 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   A(b.actA, (size_t)kMaxResid);
   A(b.actB, (size_t)kMaxResid);
   A(b.kIter, 1);
+  A(b.vel0, n);
+  A(b.rerun, nScenes);
   A(b.itersUsed, nScenes);
   {
     uint8_t* blob = nullptr;
@@ -814,6 +905,7 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
             cudaMemset(b.lamPrev, 0, 4 * n) == cudaSuccess && cudaMemset(b.lamWarm, 0, 4 * n) == cudaSuccess &&
             cudaMemset(b.done, 0, sizeof(int) * nScenes) == cudaSuccess &&
             cudaMemset(b.actA, 0, sizeof(uint32_t) * kMaxResid) == cudaSuccess &&
+            cudaMemset(b.rerun, 0, sizeof(int) * nScenes) == cudaSuccess &&
             cudaMemset(b.actB, 0, sizeof(uint32_t) * kMaxResid) == cudaSuccess &&
             cudaMemset(b.itersUsed, 0, sizeof(int) * nScenes) == cudaSuccess &&
             cudaMemset(b.resid, 0, sizeof(double) * nScenes * kMaxResid) == cudaSuccess &&
@@ -1462,6 +1554,17 @@ int xpbi_set_max_iterations(xpbi_sim* sim, int32_t max_iterations) {
     return fail(XPBI_ERR_INVALID, "max_iterations must be 0.." + std::to_string(kMaxResid - 1));
   sim->maxIters = max_iterations;
   sim->dirty = true;
+  return XPBI_OK;
+}
+
+int xpbi_read_fallback(xpbi_sim* sim, uint32_t scene, int32_t* resolved) {
+  XPBI_TRY(checkSim(sim));
+  if (scene >= sim->sc.size()) return fail(XPBI_ERR_INVALID, "scene index out of range");
+  if (!resolved) return fail(XPBI_ERR_INVALID, "resolved is NULL");
+  XPBI_TRY(xpbi_synchronize(sim));
+  int r = 0;
+  XPBI_CK(cudaMemcpy(&r, sim->b.rerun + scene, sizeof(int), cudaMemcpyDeviceToHost));
+  *resolved = r;
   return XPBI_OK;
 }
 

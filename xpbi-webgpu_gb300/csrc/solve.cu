@@ -583,6 +583,15 @@ __device__ __forceinline__ bool sceneDone(const Bufs& b, uint32_t i) {
   return b.done[s] != 0;
 }
 
+// Whether slot i's scene iterates at iteration k: below its budget and not
+// stopped, or in the plain re-solve (flags & kRerun) marked for it and below
+// its own iteration count.
+__device__ __forceinline__ bool iterating(const Bufs& b, const SceneDev& S, uint32_t i, int k, int flags) {
+  const uint32_t s = b.S > 1 ? (uint32_t)b.sceneOf[i] : 0u;
+  if (flags & kRerun) return b.rerun[s] != 0 && k < S.plainIterations;
+  return k < S.iterations && b.done[s] == 0;
+}
+
 // Largest solid displacement dt |v| per scene entering iteration k (slot
 // k & 1 of solidDisp, cleared by solveB(k - 1) or at the substep's start).
 // Called by every thread of the warp before any of them leaves: the lanes of
@@ -764,7 +773,7 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveA(Bufs b, int k, const f
   const bool measure = kTrack && (flags & kMeasureOnly) != 0;  // measure passes are tracked ones
   const bool warm0 = (flags & kWarm) != 0 && k == 0;
   const float4 pi = b.posS[i];
-  const bool active = measure || (k < S.iterations && !sceneDone(b, i));
+  const bool active = measure || iterating(b, S, i, k, flags);
   // active set (one lane per slot): from iteration 1 a solid whose inputs
   // did not change keeps its residual and takes no impulse
   const bool act = kTrack && G == 1 && (flags & kActive) != 0 && k > 0;
@@ -1163,7 +1172,7 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveB(Bufs b, int k, const f
   const float4 pi = posS[i];
   const bool track = (flags & kTrackResid) != 0;
   const bool measure = (flags & kMeasureOnly) != 0;
-  if (!measure && (k >= S.iterations || sceneDone(b, i))) {
+  if (!measure && !iterating(b, S, i, k, flags)) {
     if (lane == 0) {
       velOut[i] = vi4;
       if (writeXc) {
@@ -1468,12 +1477,12 @@ __device__ __forceinline__ bool pbfActive(const SceneDev& S, int k) {
 // the current cell with predicted positions and records, in order, the
 // predicted neighbours of this pass: all of them for water, the water ones
 // for solids (the pairs pbfB uses, simkernels.js:457-458).
-__global__ void XPBI_LB_PBF k_pbfA(Bufs b, int k) {
+__global__ void XPBI_LB_PBF k_pbfA(Bufs b, int k, int flags) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.N) return;
   const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
-  if (!pbfActive(S, k)) return;
+  if (!pbfActive(S, k) || ((flags & kRerun) && !b.rerun[sceneIndex(b, cx)])) return;
   const float4* __restrict__ xcS = b.xc;
   const float4 pi = b.posS[i];
   const bool iWater = waterW(pi.w);
@@ -1574,7 +1583,7 @@ __global__ void XPBI_LB_PBF k_pbfB(Bufs b, int k, const float4* velIn, float4* v
   const Ctx cx = ctxOf(b, i);
   const SceneDev& S = *cx.scene;
   const float4 vi4 = velIn[i];
-  if (!pbfActive(S, k)) {
+  if (!pbfActive(S, k) || ((flags & kRerun) && !b.rerun[sceneIndex(b, cx)])) {
     velOut[i] = vi4;
     return;
   }
@@ -1727,6 +1736,34 @@ __global__ void k_loop_next(Bufs b, cudaGraphConditionalHandle h) {
   }
 }
 
+// ---------------------------------------------------------------- plain re-solve
+// The judge of an early-stopped solve: a scene that did not stop within its
+// iteration cap (its residuals never reached the plain solve's tolerances)
+// is re-solved with the reference solve from the substep's input. Marks
+// those scenes and, inside a graph, sets the condition of the node whose
+// body runs the re-solve (nothing runs when every scene stopped).
+__global__ void k_judge(Bufs b, cudaGraphConditionalHandle h, int setCond) {
+  bool any = false;
+  for (uint32_t s = threadIdx.x; s < b.S; s += blockDim.x) {
+    const bool fail = b.done[s] == 0 && b.scenes[s].residTol > 0.f && b.scenes[s].plainIterations > 0;
+    b.rerun[s] = fail ? 1 : 0;
+    any |= fail;
+  }
+  any = __syncthreads_or(any) != 0;
+  if (threadIdx.x == 0 && setCond) cudaGraphSetConditional(h, any ? 1u : 0u);
+}
+// the re-solved scenes start again from the velocities entering iteration 0
+__global__ void k_restore(Bufs b, float4* __restrict__ vel) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.N) return;
+  const uint32_t s = b.S > 1 ? (uint32_t)b.sceneOf[i] : 0u;
+  if (b.rerun[s]) vel[i] = b.vel0[i];
+}
+__global__ void k_copy_vel(uint32_t n, const float4* __restrict__ src, float4* __restrict__ dst) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i];
+}
+
 inline unsigned grid(uint32_t n) { return (unsigned)((n + kThreads - 1) / kThreads); }
 inline unsigned gridOf(uint32_t n, int block) { return (unsigned)((n + (uint32_t)block - 1) / (uint32_t)block); }
 
@@ -1874,9 +1911,16 @@ void launch_solveB_list(const Bufs& b, int k, float4* vel, int flags, int varian
     default: solveBActiveVariant<0>(b, k, vel, 0, flags, true, st); break;
   }
 }
-void launch_pbfA(const Bufs& b, int k, const float4* velIn, cudaStream_t st) {
+void launch_pbfA(const Bufs& b, int k, const float4* velIn, int flags, cudaStream_t st) {
   (void)velIn;  // predicted positions were stored by the preceding solveB
-  k_pbfA<<<grid(b.N), kThreads, 0, st>>>(b, k);
+  k_pbfA<<<grid(b.N), kThreads, 0, st>>>(b, k, flags);
+}
+void launch_judge(const Bufs& b, cudaGraphConditionalHandle h, bool setCond, cudaStream_t st) {
+  k_judge<<<1, 256, 0, st>>>(b, h, setCond ? 1 : 0);
+}
+void launch_restore(const Bufs& b, float4* vel, cudaStream_t st) { k_restore<<<grid(b.N), kThreads, 0, st>>>(b, vel); }
+void launch_copy_vel(const Bufs& b, const float4* src, float4* dst, cudaStream_t st) {
+  k_copy_vel<<<grid(b.N), kThreads, 0, st>>>(b.N, src, dst);
 }
 void launch_pbfB(const Bufs& b, int k, const float4* velIn, float4* velOut, int flags, cudaStream_t st) {
   k_pbfB<<<grid(b.N), kThreads, 0, st>>>(b, k, velIn, velOut, flags);

@@ -31,6 +31,7 @@ constexpr int kStoredC = 8;            // iteration 0 reads the constraint the f
 constexpr int kMarkMoved = 16;         // a slot whose velocity changed marks itself (and, if solid, its solid
                                        // neighbours) as changed for the next iteration
 constexpr int kActive = 32;            // iteration k >= 1 visits only the slots whose inputs changed
+constexpr int kRerun = 64;             // the plain re-solve of the scenes an early-stopped solve failed
 constexpr int kIterDevice = -1000000;  // a kernel's iteration argument: read it from Bufs::kIter (device loop)
 constexpr uint32_t kNbrOverflow = 0xffffffffu;
 constexpr uint32_t kWaterBit = 0x80000000u;
@@ -76,6 +77,7 @@ struct SceneDev {
   int iterations;           // XPBI Jacobi iterations this substep (an early-stopped solve's cap)
   int pbfIterations;        // PBF passes (first k iterations)
   int pbfUntil;             // iterations k < pbfUntil run a PBF pass (the scene's own schedule)
+  int plainIterations;      // the scene's own iteration count (the plain re-solve's budget)
   int hasWater;
   float residTol;           // early stop at |r_k| <= residTol |C(v_pred)|; <= 0: never
   float residTolC;          // ... and |contact_k| <= residTolC |contact_0|
@@ -160,6 +162,8 @@ struct Bufs {
   uint32_t* actA;       // [kMaxResid] solid slots solveA evaluated, per iteration (listA's length)
   uint32_t* actB;       // [kMaxResid] slots solveB updated, per iteration (listB's length)
   int* kIter;           // [1] iteration of the device loop's current pass (kIterDevice)
+  float4* vel0;         // [N] velocities entering iteration 0 (the plain re-solve starts from them)
+  int* rerun;           // [S] 1: the early-stopped solve missed its tolerances, re-solved plainly
   int* itersUsed;       // [S] iterations whose update was applied
   void* netBlob;        // packed network weights
   SceneDev* scenes;     // [S]
@@ -198,7 +202,13 @@ cudaError_t mlp_forward(const float* dX, uint32_t rows, const void* dBlob, float
                         cudaStream_t st, bool skipZero = false);
 void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, int flags, int variant,
                    int lanes, cudaStream_t st);
-void launch_pbfA(const Bufs& b, int k, const float4* velIn, cudaStream_t st);
+void launch_pbfA(const Bufs& b, int k, const float4* velIn, int flags, cudaStream_t st);
+// the plain re-solve: judge marks the scenes whose early-stopped solve did
+// not stop (sets the graph's condition when setCond), restore resets their
+// velocities in `vel` to vel0, copy moves every slot's velocity src -> dst
+void launch_judge(const Bufs& b, cudaGraphConditionalHandle h, bool setCond, cudaStream_t st);
+void launch_restore(const Bufs& b, float4* vel, cudaStream_t st);
+void launch_copy_vel(const Bufs& b, const float4* src, float4* dst, cudaStream_t st);
 // active set, iterations without a PBF pass: compact the changed solids
 // (which = 0, listA) or the changed and impulse-receiving slots (which = 1,
 // listB), then run solveA / solveB over the list

@@ -307,6 +307,13 @@ class Simulation:
         check(lib().xpbi_read_contact_residuals(self._h, scene, out.ctypes.data_as(C.POINTER(C.c_double)), 256))
         return _written(out)
 
+    def read_fallback(self, scene: int = 0) -> bool:
+        """Whether the last substep re-solved the scene plainly (its
+        early-stopped solve missed the tolerances within its cap)."""
+        r = C.c_int32()
+        check(lib().xpbi_read_fallback(self._h, scene, C.byref(r)))
+        return bool(r.value)
+
     def set_max_iterations(self, max_iterations: int):
         """Iteration cap of an early-stopped solve (0: the scene's count)."""
         check(lib().xpbi_set_max_iterations(self._h, int(max_iterations)))
