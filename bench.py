@@ -555,6 +555,41 @@ def run_xpbi(args, rank: int, world: int):
         dist.destroy_process_group()
 
 
+def run_profile_region(args):
+    """For ncu --profile-from-start off: the learned solve of the workload set
+    up as the bench line's (plain preroll, the plain solve's tolerances from
+    tracked substeps, network warm start, active set, iteration cap), three
+    warm-up substeps from its graph, then two substeps inside
+    cudaProfilerStart/Stop, replayed from the graph (`graph`; ncu times it
+    whole) or enqueued launch by launch (`eager`; the same kernels, with the
+    iterations past the stop enqueued as launches that find nothing to do)."""
+    import torch
+    torch.cuda.set_device(0)
+    xp, scenes, _ = workload(args.workload, 0, 1)
+    stream = torch.cuda.Stream()
+    sim, has_water = make_sim(xp, scenes, stream, args.preroll)
+    sim.set_solver(0, 0.0, True, True)
+    rel, relc, _ = residual_stats(sim, has_water, len(scenes), args.residual_substeps)
+    tau, tau_c = float(np.median(rel)), float(np.median(relc))
+    tw = importlib.import_module("xpbi-webgpu_gb300.train_warm")
+    sim.set_network(tw.load_weights())
+    sim.set_active_set(args.active_share)
+    sim.set_max_iterations(args.max_iterations)
+    sim.set_solver(1, tau, False, False, contact_rel_tol=tau_c)
+    sim.step(3, -1, has_water)
+    sim.synchronize()
+    torch.cuda.profiler.start()
+    for _ in range(2):
+        if args.profile_region == "graph":
+            sim.step(1, -1, has_water)
+        else:
+            sim.encode_substep(-1, has_water)
+    sim.synchronize()
+    torch.cuda.profiler.stop()
+    print(json.dumps({"profile_region": args.profile_region, "workload": args.workload, "rel_tol": tau,
+                      "contact_rel_tol": tau_c}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -579,6 +614,9 @@ def main():
     ap.add_argument("--max-iterations", type=int, default=30,
                     help="iteration cap of the early-stopped solves (they stop once both residuals reach the plain "
                          "solve's; the plain solve runs its fixed 15)")
+    ap.add_argument("--profile-region", choices=["graph", "eager"], default=None,
+                    help="set up the learned solve and run two substeps between cudaProfilerStart/Stop (for ncu "
+                         "--profile-from-start off); prints no bench line")
     ap.add_argument("--no-ablation", action="store_true",
                     help="skip the learned solve's ablation lines (network alone, active set alone)")
     args = ap.parse_args()
@@ -589,7 +627,11 @@ def main():
         args.preroll = 100 if (args.solver == "learned" or args.impl == "reference") else 0
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
-    if args.impl == "reference":
+    if args.profile_region:
+        if args.preroll is None or args.preroll == 0:
+            args.preroll = 100
+        run_profile_region(args)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_xpbi(args, rank, world)
