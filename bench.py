@@ -349,6 +349,31 @@ def reached_fraction(rel, relc, tau: float, tau_c: float) -> float:
     return float(np.mean((r <= tau * 1.0001) & (c <= tau_c * 1.0001))) if len(r) else 0.0
 
 
+def other_configs(xp, stream, args) -> dict:
+    """The plain solve of the other benchmark configs, measured in the same
+    run (one GPU): the 16k sand column (10 iterations), the 113k NACC
+    snowball (20), the 256-scene mixed batch (~4.4M particles, 10-20 per
+    scene), each from its initial state, autotuned, `args.steps` graph
+    replays timed with CUDA events after `args.warmup`."""
+    out = {}
+    for name, scenes in (("sand_column_16k", [xp.scenes.config_sand_column()]),
+                         ("nacc_snowball_113k", [xp.scenes.config_nacc_snowball()]),
+                         ("batch256", xp.scenes.config_batch(seed=0))):
+        n = sum(len(s["positions"]) for s in scenes)
+        sim, hw = make_sim(xp, scenes, stream, 0)
+        sim.set_solver(0, 0.0, False, False)
+        sim.autotune(-1, hw, repeats=3)
+        sim.step(args.warmup, -1, hw)
+        sim.synchronize()
+        ms = timed_steps(sim, hw, args.steps, stream, None)
+        sim.close()
+        its = sorted({s["iterations"] for s in scenes})
+        out[name] = {"value": n * args.steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / args.steps,
+                     "particles": n, "scenes": len(scenes), "solver": "plain",
+                     "iterations": its if len(its) > 1 else its[0]}
+    return out
+
+
 def run_xpbi(args, rank: int, world: int):
     import torch
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -427,8 +452,8 @@ def run_xpbi(args, rank: int, world: int):
             if share > 0:
                 K = max(max(s["iterations"] for s in scenes), args.max_iterations)
                 rec["active_fraction_per_iteration"] = {
-                    "solveA": [1.0] + [round(int(x) / max(n_solid_rank, 1), 4) for x in act_a[1:K]],
-                    "solveB": [1.0] + [round(int(x) / max(n_rank, 1), 4) for x in act_b[1:K]],
+                    "solveA": [1.0, 1.0] + [round(int(x) / max(n_solid_rank, 1), 4) for x in act_a[2:K]],
+                    "solveB": [1.0, 1.0] + [round(int(x) / max(n_rank, 1), 4) for x in act_b[2:K]],
                     "of": "solids (solveA), all particles (solveB); last tracked substep"}
             return rec, (h, c) if keep else h.close()
 
@@ -546,6 +571,8 @@ def run_xpbi(args, rank: int, world: int):
            "solvers": solvers,
            "roofline": roofline, "clocks": clk, "gpu_launches": int(round(launches * args.steps)),
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}}
+    if world == 1 and not args.no_other_configs:
+        out["other_configs"] = other_configs(xp, stream, args)
     if rank == 0 and not args.no_cpu_baseline:
         _, out["cpu_baseline"] = cpu_baseline(args.cpu_scale, args.preroll, host_threads(), args.cpu_substeps,
                                               args.cpu_budget)
@@ -617,6 +644,8 @@ def main():
     ap.add_argument("--profile-region", choices=["graph", "eager"], default=None,
                     help="set up the learned solve and run two substeps between cudaProfilerStart/Stop (for ncu "
                          "--profile-from-start off); prints no bench line")
+    ap.add_argument("--no-other-configs", action="store_true",
+                    help="skip the plain solve of the sand column, snowball and 256-scene batch configs")
     ap.add_argument("--no-ablation", action="store_true",
                     help="skip the learned solve's ablation lines (network alone, active set alone)")
     args = ap.parse_args()

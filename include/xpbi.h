@@ -280,7 +280,8 @@ int xpbi_set_solver(xpbi_sim* sim, int32_t mode, float rel_tol, float contact_re
 
 /* Active set (no counterpart in the reference): work skipping for a solve
  * with an early stop (rel_tol > 0, one lane per slot; ignored otherwise).
- * Iteration 0 runs every particle. From iteration 1 on, a solid is
+ * Iterations 0 and 1 run every particle (iteration 0 moves them all).
+ * From iteration 2 on, a solid is
  * re-evaluated only if its own velocity or a solid neighbour's moved since
  * its last evaluation (otherwise its residuals are unchanged), takes an
  * impulse only if its squared constraint residual exceeds share / nSolid of
@@ -320,7 +321,8 @@ int xpbi_read_fallback(xpbi_sim* sim, uint32_t scene, int32_t* resolved);
 
 /* Particles visited per iteration of the last substep, summed over scenes:
  * solve_a[k] = solids solveA re-evaluated, solve_b[k] = particles solveB
- * updated, for k >= 1 (iteration 0 visits every particle and records 0).
+ * updated, for k >= 2 (iterations 0 and 1 visit every particle and record
+ * 0).
  * Either pointer may be NULL; cap entries at most. */
 int xpbi_read_active_counts(xpbi_sim* sim, uint32_t* solve_a, uint32_t* solve_b, int32_t cap);
 

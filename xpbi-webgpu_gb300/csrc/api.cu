@@ -465,7 +465,7 @@ struct Recorder {
 // changed solids and the slots solveB updates compacted into lists, solveA
 // and solveB over them, the residual reduction.
 void enqueueListIteration(const Bufs& b, const Schedule& sch, int k, int aflags, cudaStream_t st, Recorder& R) {
-  const int act = kMarkMoved | kActive;
+  const int act = kInPlace | kMarkMoved | kActive;
   launch_compact(b, k, 0, st);
   R.mark(st, "compact");
   launch_solveA_list(b, k, b.velS[0], aflags | act, sch.varA, st);
@@ -644,7 +644,7 @@ cudaError_t enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Re
   cudaStreamIsCapturing(st, &capSt);
   if (sch.active && capSt == cudaStreamCaptureStatusActive) {
     int k0 = sch.K;
-    while (k0 - 1 >= 1 && !sch.pbf[k0 - 1]) --k0;
+    while (k0 - 1 >= 2 && !sch.pbf[k0 - 1]) --k0;
     if (sch.K - k0 >= 2) kLoop = k0;
   }
   for (int k = 0; k < kLoop; ++k) {
@@ -655,8 +655,11 @@ cudaError_t enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Re
     // active set: iteration 0 visits every slot and marks what moved; later
     // ones visit the marked slots; velocities update in place (solveB and
     // pbfB read no neighbour's velocity), so there is no ping-pong
-    const int act = sch.active ? (kMarkMoved | (k > 0 ? kActive : 0)) : 0;
-    if (sch.active && k > 0 && !sch.pbf[k]) {
+    // iteration 0 moves every particle, so iteration 1 visits every one
+    // (skipping from it would only add the marking); it marks what it moves
+    // for iteration 2, from which on only marked particles are visited
+    const int act = sch.active ? (kInPlace | (k >= 1 ? kMarkMoved : 0) | (k >= 2 ? kActive : 0)) : 0;
+    if (sch.active && k >= 2 && !sch.pbf[k]) {
       // no PBF pass follows: solveA and solveB run over compacted lists of
       // the slots they visit (full warps however the slots are spread);
       // velocities stay in velS[0] (in place from iteration 0 on)
@@ -677,7 +680,7 @@ cudaError_t enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Re
     if (sch.pbf[k]) {
       launch_pbfA(b, k, b.velS[in], 0, st);
       R.mark(st, "pbfA");
-      launch_pbfB(b, k, b.velS[in], b.velS[in ^ (sch.active ? 0 : 1)], sch.active ? kMarkMoved : 0, st);
+      launch_pbfB(b, k, b.velS[in], b.velS[in ^ (sch.active ? 0 : 1)], sch.active && k >= 1 ? kMarkMoved : 0, st);
       R.mark(st, "pbfB");
       if (!sch.active) in ^= 1;
     }

@@ -610,7 +610,7 @@ __device__ __forceinline__ void recordSolidDisp(const Bufs& b, uint32_t i, int k
 // the reference solve). A slot's constraint depends on its own and its solid
 // neighbours' velocities, its contact correction on the predicted positions
 // of its solid neighbours: if none of those changed since the slot was last
-// evaluated, its residuals are unchanged too. So from iteration 1 on
+// evaluated, its residuals are unchanged too. So from iteration 2 on
 //   - solveA evaluates only the solids marked as changed (dirty); a solid
 //     whose residual is within the scene's per-slot threshold takes no
 //     impulse (its multiplier stays), the others update as the reference
@@ -622,7 +622,9 @@ __device__ __forceinline__ void recordSolidDisp(const Bufs& b, uint32_t i, int k
 //     neighbours as changed for the next iteration (as pbfB does);
 //   - residuals of slots not visited keep their last values, so the scene's
 //     residual sums and the early stop see every slot.
-// Iteration 0 runs every slot. The per-slot thresholds (formed once the
+// Iterations 0 and 1 run every slot (iteration 0 moves every particle, so
+// skipping in iteration 1 would find nothing to skip); iteration 1 starts
+// the marking. The per-slot thresholds (formed once the
 // iteration-0 sums are known) give each settled slot an equal share of
 // asShare times the scene's residual budget, so settled slots alone can
 // never hold the scene above its tolerance. The velocity scale is the same
@@ -774,7 +776,7 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveA(Bufs b, int k, const f
   const bool warm0 = (flags & kWarm) != 0 && k == 0;
   const float4 pi = b.posS[i];
   const bool active = measure || iterating(b, S, i, k, flags);
-  // active set (one lane per slot): from iteration 1 a solid whose inputs
+  // active set (one lane per slot): from iteration 2 a solid whose inputs
   // did not change keeps its residual and takes no impulse
   const bool act = kTrack && G == 1 && (flags & kActive) != 0 && k > 0;
   bool changed = true;
@@ -1292,7 +1294,7 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveB(Bufs b, int k, const f
 // solveB under the active set (one lane per slot; the launch passes
 // velOut == velIn: a slot reads only its own velocity, so the update is in
 // place and slots not visited keep theirs without a copy). flags & kActive
-// (iterations >= 1): only slots marked as changed (dirty) or receiving a
+// (iterations >= 2): only slots marked as changed (dirty) or receiving a
 // neighbour's impulse (bmark) run; a changed slot re-evaluates its contact
 // correction and applies it only above the scene's per-slot threshold, a
 // slot that only receives impulses keeps its (unchanged, unapplied)
@@ -1438,7 +1440,7 @@ __device__ __forceinline__ void solveBActiveSlot(const Bufs& b, int k, float4* _
 // solveB under the active set (one lane per slot; the launch passes one
 // velocity array: a slot reads only its own velocity, so the update is in
 // place and slots not visited keep theirs without a copy). flags & kActive
-// (iterations >= 1): only slots marked as changed (dirty) or receiving a
+// (iterations >= 2): only slots marked as changed (dirty) or receiving a
 // neighbour's impulse (bmark) run; a changed slot re-evaluates its contact
 // correction and applies it only above the scene's per-slot threshold, a
 // slot that only receives impulses keeps its (unchanged, unapplied)
@@ -1856,7 +1858,7 @@ void solveAListVariant(const Bufs& b, int k, const float4* velIn, int flags, cud
 void launch_solveB(const Bufs& b, int k, const float4* velIn, float4* velOut, bool writeXc, int flags, int variant,
                    int lanes, cudaStream_t st) {
   const int wx = writeXc ? 1 : 0;
-  if (flags & (kActive | kMarkMoved)) {  // the active set: in place, one lane per slot
+  if (flags & (kInPlace | kActive | kMarkMoved)) {  // the active set: in place, one lane per slot
     float4* vel = velOut;
     switch (variant) {
       case 1: solveBActiveVariant<1>(b, k, vel, wx, flags, false, st); break;

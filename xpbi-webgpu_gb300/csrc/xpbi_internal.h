@@ -32,6 +32,7 @@ constexpr int kMarkMoved = 16;         // a slot whose velocity changed marks it
                                        // neighbours) as changed for the next iteration
 constexpr int kActive = 32;            // iteration k >= 1 visits only the slots whose inputs changed
 constexpr int kRerun = 64;             // the plain re-solve of the scenes an early-stopped solve failed
+constexpr int kInPlace = 128;          // solveB of the active set: in place, one lane per slot
 constexpr int kIterDevice = -1000000;  // a kernel's iteration argument: read it from Bufs::kIter (device loop)
 constexpr uint32_t kNbrOverflow = 0xffffffffu;
 constexpr uint32_t kWaterBit = 0x80000000u;

@@ -333,7 +333,7 @@ class Simulation:
 
     def read_active_counts(self, cap: int = 129):
         """(solveA re-evaluations, solveB updates) per iteration of the last
-        substep, summed over scenes (iteration 0 visits everything: 0)."""
+        substep, summed over scenes (iterations 0 and 1 visit everything: 0)."""
         a = np.zeros(cap, np.uint32)
         b = np.zeros(cap, np.uint32)
         check(lib().xpbi_read_active_counts(self._h, _uptr(a), _uptr(b), cap))
