@@ -680,7 +680,8 @@ cudaError_t enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Re
     if (sch.pbf[k]) {
       launch_pbfA(b, k, b.velS[in], 0, st);
       R.mark(st, "pbfA");
-      launch_pbfB(b, k, b.velS[in], b.velS[in ^ (sch.active ? 0 : 1)], sch.active && k >= 1 ? kMarkMoved : 0, st);
+      launch_pbfB(b, k, b.velS[in], b.velS[in ^ (sch.active ? 0 : 1)],
+                  sch.active ? (kInPlace | (k >= 1 ? kMarkMoved : 0)) : 0, st);
       R.mark(st, "pbfB");
       if (!sch.active) in ^= 1;
     }

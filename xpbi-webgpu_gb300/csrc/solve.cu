@@ -1319,6 +1319,16 @@ __device__ __forceinline__ void solveBActiveSlot(const Bufs& b, int k, float4* _
     }
     return;
   }
+  // water: solveB only applies the boundary to it, which after iteration 0
+  // the PBF pass that moved it has already done (pbfB folds it in)
+  if (k > 0 && waterW(pi.w)) {
+    if (writeXc) {
+      const float4 vi4 = vel[i];
+      const V3 xc = xyz(pi) + S.dt * xyz(vi4);
+      b.xc[i] = make_float4(xc.x, xc.y, xc.z, pi.w);
+    }
+    return;
+  }
   const bool skip = (flags & kActive) != 0 && k > 0;
   bool changed = true;
   if (skip) {
@@ -1634,16 +1644,20 @@ __global__ void XPBI_LB_PBF k_pbfB(Bufs b, int k, const float4* velIn, float4* v
     });
   }
   const float scale = iWater ? 1.f : 0.5f;
-  const V3 v = xyz(vi4) + dp * (scale / S.dt);
+  V3 v = xyz(vi4) + dp * (scale / S.dt);
+  // active set: a water particle's boundary, which the next solveB would
+  // apply to the velocity this pass leaves (its only work on water), is
+  // applied here from the same inputs, so that solveB need not visit water
+  if ((flags & kInPlace) && iWater) v = applyBoundary(S, xyz(pi) + S.dt * v, v, xyz(pi), mWi.boundFriction);
   velOut[i] = make_float4(v.x, v.y, v.z, vi4.w);
-  // active set: the next iteration revisits a slot this pass moved (and a
-  // moved solid's solid neighbours, whose constraint and contact inputs it is)
-  if (flags & kMarkMoved) {
+  // active set: the next iteration revisits a solid this pass moved and its
+  // solid neighbours, whose constraint and contact inputs it is
+  if ((flags & kMarkMoved) && !iWater) {
     const V3 dvel = v - xyz(vi4);
     if (dot(dvel, dvel) > b.thr[3 * (uint32_t)(cx.scene - b.scenes) + 2]) {
       uint8_t* __restrict__ dn = b.dirty[(k + 1) & 1];
       dn[i] = 1;
-      if (!iWater) markSolidNbrs(b, cx, i, xyz(pi), dn);
+      markSolidNbrs(b, cx, i, xyz(pi), dn);
     }
   }
 }
