@@ -376,6 +376,42 @@ int xpbi_mlp_grad(const float* X, const float* T, uint32_t rows, const float* pa
 int xpbi_mlp_train(const float* X, const float* T, uint32_t rows, float* params, int32_t steps, uint32_t batch,
                    float lr, float* loss_history);
 
+/* ---- scene sampling on the device (web/js/scenes.js:7-38) ----
+ * The reference samples its scenes in JavaScript: sampleBox puts a lattice
+ * point at every cell centre lo + (i + 0.5) h, i < max(1, Math.round(extent
+ * / h)) per axis; sampleSphere keeps the points c - r + i h, i <= ceil(2 r /
+ * h), with Math.hypot(p - c) <= r; each coordinate gets
+ * (Math.random() - 0.5) * jitter * h. xpbi_sample_shapes runs the same loops
+ * on the GPU for scenes too large to sample quickly on the host: the lattice
+ * points are the reference's bit for bit (f64, one rounding per operation,
+ * Math.hypot as V8 evaluates it), numbered in its loop order (z outer, x
+ * inner; shapes in order), and the jitter's uniforms come from
+ * Philox-4x32-10 keyed by `seed` (low word, high word) with counter
+ * (particle number, 0 or 1, 0, 0): x and y from the first block, z from the
+ * second, each as a 53-bit double from two words. */
+enum { XPBI_SHAPE_BOX = 0, XPBI_SHAPE_SPHERE = 1 };
+typedef struct xpbi_shape {
+  int32_t kind;          /* XPBI_SHAPE_BOX or XPBI_SHAPE_SPHERE */
+  double lo[3], hi[3];   /* box corners (sampleBox's min, max) */
+  double centre[3];      /* sphere centre */
+  double radius;         /* sphere radius */
+  uint32_t mat_id;       /* material index of every particle of the shape */
+  float state0;          /* initial plastic state */
+  double jitter;         /* fraction of h (scenes.js default 0.2) */
+} xpbi_shape;
+
+/* Samples the shapes at spacing h. *count receives the particle count;
+ * with positions NULL nothing else is written (a sizing call). Otherwise
+ * capacity must be at least the count, and positions (3 floats per
+ * particle), mat_ids and states (either may be NULL) receive the particles
+ * in host memory. Synchronous; allocates temporary device memory. */
+int xpbi_sample_shapes(const xpbi_shape* shapes, uint32_t n_shapes, double h, uint64_t seed, uint32_t capacity,
+                       float* positions, uint32_t* mat_ids, float* states, uint32_t* count);
+
+/* Philox-4x32-10 (Salmon et al., SC 2011) on the host, the generator
+ * xpbi_sample_shapes uses: out = the block for `counter` under `key`. */
+int xpbi_philox4x32_10(const uint32_t counter[4], const uint32_t key[2], uint32_t out[4]);
+
 /* ---- cell sort without allocation (no counterpart in the reference) ----
  * For callers that own every byte of device memory and cannot let a library
  * allocate: engines and plugins that hand out buffers from their own fixed

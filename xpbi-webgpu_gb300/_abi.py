@@ -33,7 +33,7 @@ EXPORTS = (
     "xpbi_render", "xpbi_set_lanes", "xpbi_read_positions_async", "xpbi_test_wait_expiry",
     "xpbi_sort_cells_noalloc_status", "xpbi_test_noalloc_wait_expiry", "xpbi_read_particle_residuals",
     "xpbi_set_active_set", "xpbi_read_active_counts", "xpbi_set_max_iterations",
-    "xpbi_read_fallback",
+    "xpbi_read_fallback", "xpbi_sample_shapes", "xpbi_philox4x32_10",
 )
 
 
@@ -70,6 +70,11 @@ class Params(C.Structure):
                 ("omega", C.c_float), ("contact_omega", C.c_float), ("pbf_eps", C.c_float),
                 ("s_corr_k", C.c_float), ("time", C.c_float), ("k_damp", C.c_float),
                 ("pbf_iterations", C.c_int32)]
+
+
+class Shape(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("lo", C.c_double * 3), ("hi", C.c_double * 3), ("centre", C.c_double * 3),
+                ("radius", C.c_double), ("mat_id", C.c_uint32), ("state0", C.c_float), ("jitter", C.c_double)]
 
 
 _lib = None
@@ -114,6 +119,9 @@ _SIGS = {
     "xpbi_set_active_set": (C.c_int, [_P, C.c_float]),
     "xpbi_set_max_iterations": (C.c_int, [_P, C.c_int32]),
     "xpbi_read_fallback": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_int32)]),
+    "xpbi_sample_shapes": (C.c_int, [C.POINTER(Shape), C.c_uint32, C.c_double, C.c_uint64, C.c_uint32, _F32P,
+                                     _U32P, _F32P, _U32P]),
+    "xpbi_philox4x32_10": (C.c_int, [_U32P, _U32P, _U32P]),
     "xpbi_read_active_counts": (C.c_int, [_P, _U32P, _U32P, C.c_int32]),
     "xpbi_read_contact_residuals": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_double), C.c_int32]),
     "xpbi_autotune": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32), _F32P, C.c_int32]),

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libxpbi.so")
-SOURCES = ["api.cu", "api_mlp.cu", "sort.cu", "solve.cu", "mlp.cu", "noalloc.cu", "render.cu"]
+SOURCES = ["api.cu", "api_mlp.cu", "sort.cu", "solve.cu", "mlp.cu", "noalloc.cu", "render.cu", "sample.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
