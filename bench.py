@@ -362,7 +362,7 @@ def other_configs(xp, stream, args) -> dict:
         n = sum(len(s["positions"]) for s in scenes)
         sim, hw = make_sim(xp, scenes, stream, 0)
         sim.set_solver(0, 0.0, False, False)
-        sim.autotune(-1, hw, repeats=3)
+        tuned_o = sim.autotune(-1, hw, repeats=3)
         sim.step(args.warmup, -1, hw)
         sim.synchronize()
         ms = timed_steps(sim, hw, args.steps, stream, None)
@@ -370,7 +370,10 @@ def other_configs(xp, stream, args) -> dict:
         its = sorted({s["iterations"] for s in scenes})
         out[name] = {"value": n * args.steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / args.steps,
                      "particles": n, "scenes": len(scenes), "solver": "plain",
-                     "iterations": its if len(its) > 1 else its[0]}
+                     "iterations": its if len(its) > 1 else its[0],
+                     "autotuned_variants": {"solveA": tuned_o["solveA"], "solveB": tuned_o["solveB"],
+                                            "solveA_ms": [round(x, 4) for x in tuned_o["solveA_ms"]],
+                                            "solveB_ms": [round(x, 4) for x in tuned_o["solveB_ms"]]}}
     return out
 
 
