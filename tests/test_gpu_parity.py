@@ -254,21 +254,46 @@ def _clump(xp, sc, oracle, warm, count, material_kind, lanes=0):
         sim.encode_substep(it, sc["hasWater"])
         s1 = sim.read_state()
     assert len(idx) == count
-    return s0, s1, ref, ref64, p
+    return s0, s1, ref, ref64, p, centre.astype(np.float64)
+
+
+# A clump of particles 0.3 h across is an ill-conditioned solve: inside it and
+# within two kernel supports (2 h each) of it the f32 oracle is itself ~0.3 of
+# the peak velocity away from the f64 oracle, so there the comparison runs
+# through the noise envelope. Beyond that the substep is an ordinary one: at
+# three supports and more the GPU must match the f32 oracle to FAR_TOL of each
+# field's largest magnitude (measured: <= 1.4e-6 for the velocities).
+FAR_SUPPORTS = 3.0
+FAR_TOL = 1e-5
+
+
+def _far_field(s1, ref, centre, h, min_count):
+    d = np.linalg.norm(s1["pos"][:, :3].astype(np.float64) - centre, axis=1) / (2.0 * h)
+    far = d >= FAR_SUPPORTS
+    assert far.sum() >= min_count
+    for k in ("pos", "vel", "F", "L"):
+        a = s1[k].reshape(len(d), -1).astype(np.float64)
+        b = ref[k].reshape(len(d), -1).astype(np.float64)
+        if k in ("pos", "vel"):
+            a, b = a[:, :3], b[:, :3]
+        err = np.abs(a[far] - b[far]).max() / max(np.abs(b).max(), 1e-30)
+        assert err <= FAR_TOL, (k, err)
 
 
 @pytest.mark.parametrize("lanes", [1, 2, 4])
 def test_crowded_clump_sand(xp, oracle, built_lib, lanes):
     sc = xp.scenes.config_sand_column()
-    s0, s1, ref, ref64, p = _clump(xp, sc, oracle, 0, 150, 1, lanes)
+    s0, s1, ref, ref64, p, centre = _clump(xp, sc, oracle, 0, 150, 1, lanes)
     compare(s1, ref, ref64, perturbed=perturbed_runs(oracle, sc, s0, xp=xp, count=6, positions=True))
+    _far_field(s1, ref, centre, sc["h"], min_count=10000)
 
 
 def test_crowded_clump_water(xp, oracle, built_lib):
     sc = xp.scenes.config_dam_breach(scale=0.05)
-    s0, s1, ref, ref64, p = _clump(xp, sc, oracle, 5, 150, 6)
+    s0, s1, ref, ref64, p, centre = _clump(xp, sc, oracle, 5, 150, 6)
     compare(s1, ref, ref64, has_pbf=True,
             perturbed=perturbed_runs(oracle, sc, s0, xp=xp, count=6, positions=True))
+    _far_field(s1, ref, centre, sc["h"], min_count=40000)
 
 
 def test_batch_with_an_empty_scene(xp, oracle, built_lib):
