@@ -37,7 +37,10 @@ def test_library_philox_matches_the_oracle(built_lib):
 def test_sampler_rejects_bad_shapes(xp, built_lib):
     ds = importlib.import_module("xpbi-webgpu_gb300.device_sample")
     import pytest
-    for bad in (dict(kind=7, mat_id=0), ds.sphere([0, 0, 0], -1.0, 0), ds.box([0, 0, 0], [-1, 1, 1], 0)):
+    inf, nan = float("inf"), float("nan")
+    for bad in (dict(kind=7, mat_id=0), ds.sphere([0, 0, 0], -1.0, 0), ds.box([0, 0, 0], [-1, 1, 1], 0),
+                ds.box([-inf, 0, 0], [-inf, 1, 1], 0), ds.box([0, 0, 0], [nan, 1, 1], 0),
+                ds.sphere([inf, 0, 0], 0.1, 0), ds.sphere([0, nan, 0], 0.1, 0)):
         with pytest.raises(xp.XpbiError) as e:
             ds.sample_shapes([bad], 0.01)
         assert e.value.code == 1

@@ -199,6 +199,8 @@ extern "C" int xpbi_sample_shapes(const xpbi_shape* shapes, uint32_t n_shapes, d
     s.jitterH = in.jitter * h;
     if (in.kind == XPBI_SHAPE_BOX) {  // scenes.js:7-20
       for (int a = 0; a < 3; ++a) {
+        if (!std::isfinite(in.lo[a]) || !std::isfinite(in.hi[a]))
+          return setError(XPBI_ERR_INVALID, "box corners must be finite");
         if (!(in.hi[a] >= in.lo[a])) return setError(XPBI_ERR_INVALID, "box hi must not be below lo");
         const double e = (in.hi[a] - in.lo[a]) / h;
         if (e > 1e6) return setError(XPBI_ERR_INVALID, "box lattice too large");
@@ -208,6 +210,8 @@ extern "C" int xpbi_sample_shapes(const xpbi_shape* shapes, uint32_t n_shapes, d
       s.off = 0.5;
     } else if (in.kind == XPBI_SHAPE_SPHERE) {  // scenes.js:22-38
       if (!(in.radius > 0) || !std::isfinite(in.radius)) return setError(XPBI_ERR_INVALID, "radius must be > 0");
+      for (int a = 0; a < 3; ++a)
+        if (!std::isfinite(in.centre[a])) return setError(XPBI_ERR_INVALID, "sphere centre must be finite");
       const double nn = std::ceil(2 * in.radius / h);
       if (nn > 1e5) return setError(XPBI_ERR_INVALID, "sphere lattice too large");
       for (int a = 0; a < 3; ++a) {
@@ -236,8 +240,10 @@ extern "C" int xpbi_sample_shapes(const xpbi_shape* shapes, uint32_t n_shapes, d
           cudaMalloc(&blockStarts[q].p, sizeof(uint32_t) * blocks) != cudaSuccess)
         return setError(XPBI_ERR_OOM, "xpbi_sample_shapes: device memory");
       k_sphere_count<<<(unsigned)blocks, kThreads>>>(sd[q], h, points[q], (uint32_t*)cnt.p);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return setError(XPBI_ERR_CUDA, std::string("sphere count: ") + cudaGetErrorString(e));
       std::vector<uint32_t> c(blocks);
-      cudaError_t e = cudaMemcpy(c.data(), cnt.p, sizeof(uint32_t) * blocks, cudaMemcpyDeviceToHost);
+      e = cudaMemcpy(c.data(), cnt.p, sizeof(uint32_t) * blocks, cudaMemcpyDeviceToHost);
       if (e != cudaSuccess) return setError(XPBI_ERR_CUDA, std::string("sphere count: ") + cudaGetErrorString(e));
       uint32_t run = 0;
       for (uint64_t b = 0; b < blocks; ++b) {
@@ -274,7 +280,8 @@ extern "C" int xpbi_sample_shapes(const xpbi_shape* shapes, uint32_t n_shapes, d
     }
     k_fill<<<(kept[q] + kThreads - 1) / kThreads, kThreads>>>(sd[q], h, kept[q], (const uint64_t*)lat.p, k0, k1,
                                                              (float*)pos.p, (uint32_t*)mat.p, (float*)st.p);
-    const cudaError_t e = cudaDeviceSynchronize();  // before `lat` is freed
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();  // before `lat` is freed
     if (e != cudaSuccess) return setError(XPBI_ERR_CUDA, std::string("sampling: ") + cudaGetErrorString(e));
   }
   cudaError_t e = cudaMemcpy(positions, pos.p, 12 * total, cudaMemcpyDeviceToHost);
