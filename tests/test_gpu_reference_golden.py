@@ -10,11 +10,14 @@ result under the parity definition of parity_util (sort bit-exact, state
 within 1e-4 relative, with the f32 noise envelope of the oracle where the
 reference algorithm itself is ill-conditioned).
 
-At full size (the 1M-particle dam breach, too large for the oracle in a
-test) one substep must give a valid counting sort — a permutation in cell
-order whose cell table counts the cells of the positions it was sorted
-from — finite state inside the domain, non-positive PBF multipliers, and
-the same bytes when repeated from the same state.
+At full size (too large for the oracle in a test) — the 1M-particle dam
+breach (plain solve), the 4M-particle dam-breach mix under the learned
+solve as benchmarked, and the 256-scene mixed batch — one substep must give
+every scene a valid counting sort (a permutation in cell order whose cell
+table counts the cells of the positions it was sorted from), finite state
+inside the domain, non-positive PBF multipliers, and the same bytes when
+repeated from the same state; the learned solve must also end every scene
+within both tolerances or re-solve it plainly.
 """
 import importlib.util
 import os
@@ -69,6 +72,44 @@ def test_gpu_reproduces_reference_golden_substeps(xp, oracle, built_lib):
         print(name, {k: f"{v:.1e}" for k, v in rep.items() if "_" not in k})
 
 
+def _check_substep(s0, a, pw, label=""):
+    """One substep of a scene from state s0 to a: a counting sort (a
+    permutation in cell order, within a cell by descending previous index,
+    whose cell table counts the cells of the positions it was sorted from),
+    finite state inside the domain, non-positive PBF multipliers."""
+    n = len(s0["pos"])
+    idx = a["sortedIdx"].astype(np.int64)
+    assert np.array_equal(np.sort(idx), np.arange(n)), f"{label}: not a permutation"
+    o = pw[0:3].view(np.float32)
+    cs = pw[3:4].view(np.float32)[0]
+    dims = pw[4:7].astype(np.int64)
+    x = s0["pos"][:, :3]
+    c = np.clip(np.floor((x - o) / cs), 0, dims - 1).astype(np.int64)
+    key = c[:, 0] + c[:, 1] * dims[0] + c[:, 2] * dims[0] * dims[1]
+    ks = key[idx]
+    assert np.all(np.diff(ks) >= 0), f"{label}: not in cell order"
+    same = np.diff(ks) == 0
+    assert np.all(np.diff(idx)[same] < 0), f"{label}: within a cell, not by descending previous index"
+    counts = np.bincount(key, minlength=int(pw[7]))
+    assert np.array_equal(a["cellTab"].astype(np.int64), np.concatenate([[0], np.cumsum(counts)[:-1]])), label
+    for k in ("pos", "vel", "F", "L", "aux"):
+        assert np.all(np.isfinite(a[k])), f"{label}: {k}"
+    lo = pw[8:11].view(np.float32)
+    hi = pw[12:15].view(np.float32)
+    assert np.all(a["pos"][:, :3] >= lo) and np.all(a["pos"][:, :3] <= hi), label
+    assert np.all(a["aux"][:, 3] <= 0.0), label
+
+
+def _same(a, b, label=""):
+    for k in ("pos", "vel", "F", "L", "aux", "sortedIdx", "cellTab"):
+        assert np.array_equal(a[k], b[k]), f"{label}: repeat differs in {k}"
+
+
+def _restore(sim, states):
+    for k, st in enumerate(states):
+        sim.write_state(k, pos=st["pos"], vel=st["vel"], F=st["F"], aux=st["aux"])
+
+
 def test_full_size_substep_properties(xp, built_lib):
     sc = xp.scenes.config_dam_breach()
     p = xp.params_for(sc)
@@ -79,30 +120,91 @@ def test_full_size_substep_properties(xp, built_lib):
         s0 = sim.read_state()
         sim.encode_substep(it, True)
         a = sim.read_state()
-        sim.write_state(0, pos=s0["pos"], vel=s0["vel"], F=s0["F"], aux=s0["aux"])
+        _restore(sim, [s0])
         sim.encode_substep(it, True)
         b = sim.read_state()
         pw, _ = sim.uniforms()
-    n = len(s0["pos"])
-    for k in ("pos", "vel", "F", "L", "aux", "sortedIdx", "cellTab"):
-        assert np.array_equal(a[k], b[k]), f"repeat differs in {k}"
-    idx = a["sortedIdx"].astype(np.int64)
-    assert np.array_equal(np.sort(idx), np.arange(n)), "not a permutation"
-    o = pw[0:3].view(np.float32)
-    cs = pw[3:4].view(np.float32)[0]
-    dims = pw[4:7].astype(np.int64)
-    x = s0["pos"][:, :3]
-    c = np.clip(np.floor((x - o) / cs), 0, dims - 1).astype(np.int64)
-    key = c[:, 0] + c[:, 1] * dims[0] + c[:, 2] * dims[0] * dims[1]
-    ks = key[idx]
-    assert np.all(np.diff(ks) >= 0), "not in cell order"
-    same = np.diff(ks) == 0
-    assert np.all(np.diff(idx)[same] < 0), "within a cell, not by descending previous index"
-    counts = np.bincount(key, minlength=int(pw[7]))
-    assert np.array_equal(a["cellTab"].astype(np.int64), np.concatenate([[0], np.cumsum(counts)[:-1]]))
-    for k in ("pos", "vel", "F", "L", "aux"):
-        assert np.all(np.isfinite(a[k])), k
-    lo = pw[8:11].view(np.float32)
-    hi = pw[12:15].view(np.float32)
-    assert np.all(a["pos"][:, :3] >= lo) and np.all(a["pos"][:, :3] <= hi)
-    assert np.all(a["aux"][:, 3] <= 0.0)
+    _same(a, b)
+    _check_substep(s0, a, pw)
+
+
+def test_full_size_learned_mix_properties(xp, built_lib):
+    """The benchmark's headline path at its size: the 4M-particle dam-breach
+    mix (four 1M scenes, one handle) under the learned solve as benchmarked
+    (network warm start, active set share 0.25, iteration cap 30; in the
+    substep's graph the device while-loop and the judge's conditional
+    re-solve), one substep from the benchmark's state 100 plain substeps in
+    (the solids loaded, the water flowing): every scene's sort
+    and state valid, the same bytes when the graph substep is repeated from
+    the same state (the worklists are appended by atomics in no fixed order;
+    no result may depend on it), and every scene either within both
+    tolerances — the plain solve's final relative residuals on the same
+    substep, median over the scenes — or re-solved plainly by the judge."""
+    import importlib
+    tw = importlib.import_module("xpbi-webgpu_gb300.train_warm")
+    scenes = xp.scenes.config_dam_mix()
+    S = len(scenes)
+    with xp.Simulation(scenes) as sim:
+        for k, sc in enumerate(scenes):
+            sim.write_params(xp.params_for(sc), scene=k)
+            sim.set_schedule(k, sc["iterations"], sc["hasWater"])
+        sim.set_solver(0, 0.0, False, True)  # carries the multipliers the warm start reads
+        sim.step(100, -1, True)
+        s0 = [sim.read_state(k) for k in range(S)]
+        pw = [sim.uniforms(k)[0] for k in range(S)]
+
+        def rel(k):
+            r, _ = sim.read_residuals(k)
+            c = sim.read_contact_residuals(k)
+            return float(r[-1] / r[0]), float(c[-1] / c[0])
+
+        sim.set_solver(0, 0.0, True, False)
+        sim.step(1, -1, True)
+        plain = [rel(k) for k in range(S)]
+        tau = float(np.median([x[0] for x in plain]))
+        tau_c = float(np.median([x[1] for x in plain]))
+        assert 0.0 < tau <= 1.0 and 0.0 < tau_c <= 1.0, plain
+        _restore(sim, s0)
+        sim.set_network(tw.load_weights())
+        sim.set_active_set(0.25)
+        sim.set_max_iterations(30)
+        sim.set_solver(1, tau, True, False, contact_rel_tol=tau_c)
+        sim.step(1, -1, True)
+        a = [sim.read_state(k) for k in range(S)]
+        learned = [rel(k) for k in range(S)]
+        resolved = [sim.read_fallback(k) for k in range(S)]
+        _restore(sim, s0)
+        sim.step(1, -1, True)
+        b = [sim.read_state(k) for k in range(S)]
+    print({"tau": tau, "tau_c": tau_c, "learned": learned, "resolved": resolved})
+    for k in range(S):
+        _same(a[k], b[k], f"scene {k}")
+        _check_substep(s0[k], a[k], pw[k], f"scene {k}")
+        reached = learned[k][0] <= tau * 1.0001 and learned[k][1] <= tau_c * 1.0001
+        assert reached or resolved[k], (k, learned[k], tau, tau_c)
+
+
+def test_full_size_batch_properties(xp, built_lib):
+    """The 256-scene mixed batch (about 4M particles over 256 scenes of 2k to
+    60k particles, every plasticity model, 10 to 20 iterations each) in one
+    handle: after three graph substeps, one more gives every scene a valid
+    sort and state, and the same bytes when repeated from the same state."""
+    scenes = xp.scenes.config_batch(seed=0)
+    S = len(scenes)
+    hw = any(sc["hasWater"] for sc in scenes)
+    with xp.Simulation(scenes) as sim:
+        for k, sc in enumerate(scenes):
+            sim.write_params(xp.params_for(sc), scene=k)
+            sim.set_schedule(k, sc["iterations"], sc["hasWater"])
+        sim.step(3, -1, hw)
+        s0 = [sim.read_state(k) for k in range(S)]
+        pw = [sim.uniforms(k)[0] for k in range(S)]
+        sim.step(1, -1, hw)
+        a = [sim.read_state(k) for k in range(S)]
+        _restore(sim, s0)
+        sim.step(1, -1, hw)
+        b = [sim.read_state(k) for k in range(S)]
+    assert sum(len(x["pos"]) for x in s0) > 3_000_000
+    for k in range(S):
+        _same(a[k], b[k], f"scene {k}")
+        _check_substep(s0[k], a[k], pw[k], f"scene {k}")
