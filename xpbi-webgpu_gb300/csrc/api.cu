@@ -461,9 +461,9 @@ struct Recorder {
   }
 };
 
-// One active-set iteration without a PBF pass (k may be kIterDevice): the
-// changed solids and the slots solveB updates compacted into lists, solveA
-// and solveB over them, the residual reduction.
+// One active-set iteration's solve (k may be kIterDevice): the changed
+// solids and the slots solveB updates compacted into lists, solveA and
+// solveB over them, the residual reduction.
 void enqueueListIteration(const Bufs& b, const Schedule& sch, int k, int aflags, cudaStream_t st, Recorder& R) {
   const int act = kInPlace | kMarkMoved | kActive;
   launch_compact(b, k, 0, st);
@@ -659,22 +659,27 @@ cudaError_t enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Re
     // (skipping from it would only add the marking); it marks what it moves
     // for iteration 2, from which on only marked particles are visited
     const int act = sch.active ? (kInPlace | (k >= 1 ? kMarkMoved : 0) | (k >= 2 ? kActive : 0)) : 0;
-    if (sch.active && k >= 2 && !sch.pbf[k]) {
-      // no PBF pass follows: solveA and solveB run over compacted lists of
-      // the slots they visit (full warps however the slots are spread);
-      // velocities stay in velS[0] (in place from iteration 0 on)
+    if (sch.active && k >= 2) {
+      // solveA and solveB run over compacted lists of the slots they visit
+      // (full warps however the slots are spread); velocities stay in
+      // velS[0] (in place from iteration 0 on). Before a PBF pass every
+      // slot's predicted position is brought up to date, as the per-slot
+      // solveB would have left it.
       enqueueListIteration(b, sch, k, aflags, st, R);
-      continue;
+      if (sch.pbf[k]) {
+        launch_predict(b, b.velS[0], st);
+        R.mark(st, "predict");
+      }
     } else {
       launch_solveA(b, k, b.velS[in], aflags | stored | (act & kActive), sch.varA, sch.lanes, st);
       R.mark(st, "solveA");
       launch_solveB(b, k, b.velS[in], b.velS[in ^ (sch.active ? 0 : 1)], sch.pbf[k] != 0,
                     (sch.reduce ? kTrackResid : 0) | act, sch.varB, sch.lanes, st);
       R.mark(st, "solveB");
-    }
-    if (sch.reduce) {
-      launch_resid_reduce(b, k, (aflags & kWarm) != 0, st);
-      R.mark(st, "residual");
+      if (sch.reduce) {
+        launch_resid_reduce(b, k, (aflags & kWarm) != 0, st);
+        R.mark(st, "residual");
+      }
     }
     if (!sch.active) in ^= 1;
     if (sch.pbf[k]) {
@@ -733,8 +738,10 @@ cudaError_t enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Re
 
 int kernelsPerSubstep(const Schedule& sch) {
   int n = 5 /* count, scan, fill, bigcells, reorder */ + 1 /* computeL */ + 2 /* xsph, updateF+integrate */;
-  for (int k = 0; k < sch.K; ++k)
-    n += 2 + (sch.pbf[k] ? 2 : 0) + (sch.reduce ? 1 : 0) + (sch.active && k > 0 && !sch.pbf[k] ? 2 : 0);
+  for (int k = 0; k < sch.K; ++k) {
+    const bool list = sch.active && k >= 2;  // two compactions; before a PBF pass, the predicted positions
+    n += 2 + (sch.pbf[k] ? 2 : 0) + (sch.reduce ? 1 : 0) + (list ? 2 + (sch.pbf[k] ? 1 : 0) : 0);
+  }
   if (sch.features) n += 1;
   if (sch.mode == 1) n += 2;
   if (sch.mode == 2) n += 1;

@@ -1775,6 +1775,19 @@ __global__ void k_restore(Bufs b, float4* __restrict__ vel) {
   const uint32_t s = b.S > 1 ? (uint32_t)b.sceneOf[i] : 0u;
   if (b.rerun[s]) vel[i] = b.vel0[i];
 }
+// The PBF pass's predicted positions x + dt v of every slot from the
+// velocities as they stand: after an active-set iteration over worklists,
+// the slots it did not visit and the ones the previous PBF pass moved hold
+// older ones. The expression is solveB's when it writes them, so the
+// result is the one the per-slot kernels leave.
+__global__ void k_predict(Bufs b, const float4* __restrict__ vel) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.N) return;
+  const SceneDev& S = *ctxOf(b, i).scene;
+  const float4 pi = b.posS[i];
+  const V3 xc = xyz(pi) + S.dt * xyz(vel[i]);
+  b.xc[i] = make_float4(xc.x, xc.y, xc.z, pi.w);
+}
 __global__ void k_copy_vel(uint32_t n, const float4* __restrict__ src, float4* __restrict__ dst) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dst[i] = src[i];
@@ -1935,6 +1948,7 @@ void launch_judge(const Bufs& b, cudaGraphConditionalHandle h, bool setCond, cud
   k_judge<<<1, 256, 0, st>>>(b, h, setCond ? 1 : 0);
 }
 void launch_restore(const Bufs& b, float4* vel, cudaStream_t st) { k_restore<<<grid(b.N), kThreads, 0, st>>>(b, vel); }
+void launch_predict(const Bufs& b, const float4* vel, cudaStream_t st) { k_predict<<<grid(b.N), kThreads, 0, st>>>(b, vel); }
 void launch_copy_vel(const Bufs& b, const float4* src, float4* dst, cudaStream_t st) {
   k_copy_vel<<<grid(b.N), kThreads, 0, st>>>(b.N, src, dst);
 }

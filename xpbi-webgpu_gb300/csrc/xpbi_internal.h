@@ -210,9 +210,11 @@ void launch_pbfA(const Bufs& b, int k, const float4* velIn, int flags, cudaStrea
 void launch_judge(const Bufs& b, cudaGraphConditionalHandle h, bool setCond, cudaStream_t st);
 void launch_restore(const Bufs& b, float4* vel, cudaStream_t st);
 void launch_copy_vel(const Bufs& b, const float4* src, float4* dst, cudaStream_t st);
-// active set, iterations without a PBF pass: compact the changed solids
-// (which = 0, listA) or the changed and impulse-receiving slots (which = 1,
-// listB), then run solveA / solveB over the list
+// every slot's predicted position for pbfA from the velocities in `vel`
+void launch_predict(const Bufs& b, const float4* vel, cudaStream_t st);
+// active set, iterations from 2: compact the changed solids (which = 0,
+// listA) or the changed and impulse-receiving slots (which = 1, listB),
+// then run solveA / solveB over the list
 void launch_compact(const Bufs& b, int k, int which, cudaStream_t st);
 void launch_solveA_list(const Bufs& b, int k, const float4* velIn, int flags, int variant, cudaStream_t st);
 void launch_solveB_list(const Bufs& b, int k, float4* vel, int flags, int variant, cudaStream_t st);
