@@ -795,6 +795,8 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   b.N = (uint32_t)N;
   b.C = (uint32_t)C;
   b.S = nScenes;
+  b.maxSceneN = 0;
+  for (const SceneHost& h : s->sc) b.maxSceneN = std::max<uint32_t>(b.maxSceneN, (uint32_t)h.n);
   b.scanTiles = scan_tiles(b.C);
   const size_t n = std::max<size_t>(b.N, 1);
 #define A(ptr, cnt)                               \
@@ -846,7 +848,7 @@ int createImpl(const xpbi_scene_desc* scenes, uint32_t nScenes, xpbi_sim** out) 
   A(b.c0sq, n);
   A(b.rc, n);
   A(b.solidDisp, 2 * (size_t)nScenes);
-  A(b.residPart, (size_t)nScenes * kResidChunks * 4);
+  A(b.residPart, (size_t)nScenes * kResidBlocks * 4);
   A(b.residTicket, nScenes);
   A(b.resid, (size_t)nScenes * kMaxResid);
   A(b.residC, (size_t)nScenes * kMaxResid);

@@ -801,17 +801,20 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveA(Bufs b, int k, const f
   solveAUpdate<kTrack>(b, cx, i, pi, velIn, mi, c, k, warm0, measure, act);
 }
 
-// Active set, iterations without a PBF pass: the changed solid slots of the
-// scenes still iterating, appended to a list (warp-aggregated, in no
-// particular order: each slot's own sums keep their list order, so the
-// results do not depend on it); which = 1 lists the slots solveB updates
-// (changed or receiving an impulse). The list's length is the iteration's
-// visit count. Each thread reads the flags of 16 consecutive slots with one
-// 16-byte load per array (the flag arrays are padded to a multiple of 16),
-// checks the few flagged ones, and the warp appends its slots with one
-// atomic.
+// Active set, iterations from 2: the changed slots of the scenes still
+// iterating, appended to a list (in no particular order: each slot's own
+// sums keep their list order, so the results do not depend on it); which = 1
+// lists the slots solveB updates (changed or receiving an impulse). Only
+// solids are ever marked changed; k_solveA_list skips any water slot. The
+// list's length is the iteration's visit count. Each thread reads the flags
+// of 16 consecutive slots with one 16-byte load per array (the flag arrays
+// are padded to a multiple of 16) and checks the few flagged ones; the
+// block appends its slots with one atomic.
 constexpr int kCompactSlots = 16;
-__global__ void __launch_bounds__(kThreads) k_compact(Bufs b, int k, int which) {
+constexpr int kCompactThreads = 256;
+__global__ void __launch_bounds__(kCompactThreads) k_compact(Bufs b, int k, int which) {
+  __shared__ uint32_t warpBase[kCompactThreads / 32];
+  __shared__ uint32_t blockBase;
   k = iterK(b, k);
   const uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) * kCompactSlots;
   uint32_t take = 0;
@@ -828,23 +831,32 @@ __global__ void __launch_bounds__(kThreads) k_compact(Bufs b, int k, int which) 
       const uint32_t i = base + (uint32_t)q;
       if (i >= b.N) break;
       const uint32_t s = b.S > 1 ? (uint32_t)b.sceneOf[i] : 0u;
-      if (k < b.scenes[s].iterations && !b.done[s] && (which == 1 || !waterW(b.posS[i].w))) take |= 1u << q;
+      if (k < b.scenes[s].iterations && !b.done[s]) take |= 1u << q;
     }
   }
   const uint32_t cnt = (uint32_t)__popc(take);
-  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   uint32_t incl = cnt;
 #pragma unroll
   for (int off = 1; off < 32; off <<= 1) {
     const uint32_t n = __shfl_up_sync(0xffffffffu, incl, off);
     if (lane >= (unsigned)off) incl += n;
   }
-  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-  if (total == 0u) return;
-  uint32_t* ctr = which == 0 ? b.actA + k : b.actB + k;
-  uint32_t start = 0;
-  if (lane == 31u) start = atomicAdd(ctr, total);
-  start = __shfl_sync(0xffffffffu, start, 31) + incl - cnt;
+  if (lane == 31u) warpBase[warp] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+#pragma unroll
+    for (int q = 0; q < kCompactThreads / 32; ++q) {
+      const uint32_t t = warpBase[q];
+      warpBase[q] = run;
+      run += t;
+    }
+    blockBase = run ? atomicAdd(which == 0 ? b.actA + k : b.actB + k, run) : 0u;
+  }
+  __syncthreads();
+  if (!take) return;
+  uint32_t start = blockBase + warpBase[warp] + incl - cnt;
   uint32_t* out = which == 0 ? b.listA : b.listB;
   while (take) {
     const int q = __ffs(take) - 1;
@@ -863,9 +875,10 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveA_list(Bufs b, int k, co
   const uint32_t cnt = *(volatile const uint32_t*)(b.actA + k);
   for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < cnt; t += gridDim.x * blockDim.x) {
     const uint32_t i = b.listA[t];
+    const float4 pi = b.posS[i];
+    if (waterW(pi.w)) continue;  // water takes no constraint (none is ever marked)
     const Ctx cx = ctxOf(b, i);
     const SceneDev& S = *cx.scene;
-    const float4 pi = b.posS[i];
     recordSolidDisp(b, i, k, S.dt * length(xyz(velIn[i])));
     const uint32_t mi = matOfW(pi.w);
     const float st = b.stateS[i];
@@ -960,18 +973,19 @@ __global__ void k_warm_from_prev(Bufs b) {
   b.lamWarm[i] = b.lamPrev[i];
 }
 
-// Per-scene residual norms, deterministic, in one launch: warp w of block
-// (x, s) sums chunk 8x + w of scene s in a fixed order and stores the
-// chunk's partial sums; the last of the scene's blocks to finish (a ticket
-// counter, no waiting) adds the chunks in chunk order, so the totals do not
-// depend on which block comes last. One wave of blocks whose warps each
-// stream a chunk with float4 loads: the per-block chains of dependent loads,
-// barriers and fences are few.
+// Per-scene residual norms, deterministic, in one launch: block (x, s)
+// sums the x-th of the scene's residBlocks(n) consecutive slot ranges (at
+// least kResidPerBlock slots each, at most kResidBlocks ranges, so a large
+// scene fills the GPU with float4 loads in flight and a small one takes few
+// blocks) in a fixed order and stores the range's partial sums; the last of
+// the scene's blocks to finish (a ticket counter, no waiting) adds the
+// partials in range order, so the totals do not depend on which block comes
+// last.
 // Sums: constraint residual^2, (iteration 0) residual^2 at lambda = 0,
-// contact correction^2.
-// Chunk sums are formed in f32 (a convergence test on sums of squares needs
-// nothing finer, and f64 is slow here) in a fixed per-lane order and a fixed
-// warp butterfly; the chunks are added in f64.
+// contact correction^2, (iteration 0) velocity change^2.
+// Each thread sums in f32 in a fixed order (a convergence test on sums of
+// squares needs nothing finer, and f64 is slow here), then a fixed warp
+// butterfly; the warps of a block and the ranges of a scene are added in f64.
 //
 // k >= 0: the residuals of the state entering iteration k (early stop),
 // reduced after iteration k's update; k < 0: after the last iteration (slot
@@ -982,41 +996,49 @@ __global__ void k_warm_from_prev(Bufs b) {
 // 0's constraint residual is the linearised estimate before the warm impulse
 // is applied, so it never stops the solve.
 constexpr int kResidSums = 4;
-constexpr int kResidWarps = 8;  // chunks per block, one warp each
-static_assert(kResidChunks % kResidWarps == 0, "whole blocks of chunks");
-__global__ void __launch_bounds__(32 * kResidWarps) k_resid(Bufs b, int k, int warm) {
+constexpr int kResidThreads = 256;
+constexpr uint32_t kResidPerBlock = 4096;
+static_assert(kResidBlocks % 32 == 0, "whole lanes of partials in the final sum");
+__host__ __device__ __forceinline__ uint32_t residBlocks(uint32_t n) {
+  const uint32_t g = (n + kResidPerBlock - 1u) / kResidPerBlock;
+  return g < 1u ? 1u : (g > (uint32_t)kResidBlocks ? (uint32_t)kResidBlocks : g);
+}
+__global__ void __launch_bounds__(kResidThreads) k_resid(Bufs b, int k, int warm) {
+  __shared__ float warpSum[kResidThreads / 32][kResidSums];
   __shared__ bool lastBlock;
   k = iterK(b, k);
   const uint32_t s = blockIdx.y;
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t c = blockIdx.x * kResidWarps + (threadIdx.x >> 5);  // this warp's chunk
   const SceneDev& S = b.scenes[s];
   const uint32_t n = S.n, base = S.pBase;
-  const uint32_t lo = base + (uint32_t)(((uint64_t)n * c) / kResidChunks);
-  const uint32_t hi = base + (uint32_t)(((uint64_t)n * (c + 1)) / kResidChunks);
+  const uint32_t G = residBlocks(n);
+  if (blockIdx.x >= G) return;  // the whole block: this scene needs fewer ranges
+  const uint32_t c = blockIdx.x;
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const uint32_t lo = base + (uint32_t)(((uint64_t)n * c) / G);
+  const uint32_t hi = base + (uint32_t)(((uint64_t)n * (c + 1)) / G);
   float a = 0.f, a0 = 0.f, ac = 0.f, av = 0.f;
   const bool velSum = k == 0 && S.asShare > 0.f;  // the active set's velocity-change scale
   if (!b.done[s] || k < 0) {
-    // the chunk's 16-byte-aligned interior as float4 (the arrays start on
+    // the range's 16-byte-aligned interior as float4 (the arrays start on
     // 256-byte boundaries), its ragged ends (< 4 slots each) as scalars
     const uint32_t lo4 = min(hi, (lo + 3u) & ~3u), hi4 = max(lo4, hi & ~3u);
-    if (lo + lane < lo4) {
-      a += b.rr[lo + lane];
-      ac += b.rc[lo + lane];
-      if (k == 0) a0 += b.c0sq[lo + lane];
-      if (velSum) av += b.dv0sq[lo + lane];
+    if (lo + tid < lo4) {
+      a += b.rr[lo + tid];
+      ac += b.rc[lo + tid];
+      if (k == 0) a0 += b.c0sq[lo + tid];
+      if (velSum) av += b.dv0sq[lo + tid];
     }
-    if (hi4 + lane < hi) {
-      a += b.rr[hi4 + lane];
-      ac += b.rc[hi4 + lane];
-      if (k == 0) a0 += b.c0sq[hi4 + lane];
-      if (velSum) av += b.dv0sq[hi4 + lane];
+    if (hi4 + tid < hi) {
+      a += b.rr[hi4 + tid];
+      ac += b.rc[hi4 + tid];
+      if (k == 0) a0 += b.c0sq[hi4 + tid];
+      if (velSum) av += b.dv0sq[hi4 + tid];
     }
     const float4* __restrict__ rr4 = reinterpret_cast<const float4*>(b.rr);
     const float4* __restrict__ rc4 = reinterpret_cast<const float4*>(b.rc);
     const float4* __restrict__ c04 = reinterpret_cast<const float4*>(b.c0sq);
 #pragma unroll 4
-    for (uint32_t q = lo4 / 4u + lane; q < hi4 / 4u; q += 32u) {
+    for (uint32_t q = lo4 / 4u + tid; q < hi4 / 4u; q += kResidThreads) {
       const float4 x = rr4[q], y = rc4[q];
       a += (x.x + x.y) + (x.z + x.w);
       ac += (y.x + y.y) + (y.z + y.w);
@@ -1038,33 +1060,43 @@ __global__ void __launch_bounds__(32 * kResidWarps) k_resid(Bufs b, int k, int w
     av += __shfl_xor_sync(0xffffffffu, av, off);
   }
   if (lane == 0) {
-    double* part = b.residPart + (s * kResidChunks + c) * kResidSums;
-    part[0] = (double)a;
-    part[1] = (double)a0;
-    part[2] = (double)ac;
-    part[3] = (double)av;
+    warpSum[warp][0] = a;
+    warpSum[warp][1] = a0;
+    warpSum[warp][2] = ac;
+    warpSum[warp][3] = av;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double t[kResidSums] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int w = 0; w < kResidThreads / 32; ++w)
+#pragma unroll
+      for (int q = 0; q < kResidSums; ++q) t[q] += (double)warpSum[w][q];
+    double* part = b.residPart + ((size_t)s * kResidBlocks + c) * kResidSums;
+#pragma unroll
+    for (int q = 0; q < kResidSums; ++q) part[q] = t[q];
     __threadfence();  // the partials are visible before this block's ticket
+    lastBlock = atomicAdd(b.residTicket + s, 1u) == G - 1u;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();  // orders the warps' partials (published at the barrier) before the ticket
-    lastBlock = atomicAdd(b.residTicket + s, 1u) == gridDim.x - 1u;
-  }
-  __syncthreads();
-  if (!lastBlock || threadIdx.x >= 32u) return;
-  // the scene's last block, one warp: lane l adds chunks l, l + 32, ... in
+  if (!lastBlock || tid >= 32u) return;
+  // the scene's last block, one warp: lane l adds ranges l, l + 32, ... in
   // order (loads through L2: the other blocks' partials are not in this
   // SM's L1), then a fixed butterfly combines the lanes
   __threadfence();
   if (lane == 0) b.residTicket[s] = 0u;  // every block of this launch has taken its ticket
   if (k >= 0 && (b.done[s] || k >= S.iterations)) return;
   double ta = 0.0, ta0 = 0.0, tac = 0.0, tav = 0.0;
-  for (int q = (int)lane; q < kResidChunks; q += 32) {
-    const double* part = b.residPart + (s * kResidChunks + q) * kResidSums;
-    ta += __ldcg(part);
-    ta0 += __ldcg(part + 1);
-    tac += __ldcg(part + 2);
-    tav += __ldcg(part + 3);
+#pragma unroll
+  for (int r = 0; r < kResidBlocks / 32; ++r) {
+    const uint32_t q = lane + 32u * (uint32_t)r;
+    if (q < G) {
+      const double* part = b.residPart + ((size_t)s * kResidBlocks + q) * kResidSums;
+      ta += __ldcg(part);
+      ta0 += __ldcg(part + 1);
+      tac += __ldcg(part + 2);
+      tav += __ldcg(part + 3);
+    }
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
@@ -1853,7 +1885,7 @@ void launch_features(const Bufs& b, const float4* velIn, cudaStream_t st) {
 void launch_warm_from_net(const Bufs& b, cudaStream_t st) { k_warm_from_net<<<grid(b.N), kThreads, 0, st>>>(b); }
 void launch_warm_from_prev(const Bufs& b, cudaStream_t st) { k_warm_from_prev<<<grid(b.N), kThreads, 0, st>>>(b); }
 void launch_resid_reduce(const Bufs& b, int k, bool warm, cudaStream_t st) {
-  k_resid<<<dim3(kResidChunks / kResidWarps, b.S), 32 * kResidWarps, 0, st>>>(b, k, warm ? 1 : 0);
+  k_resid<<<dim3(residBlocks(b.maxSceneN), b.S), kResidThreads, 0, st>>>(b, k, warm ? 1 : 0);
 }
 void launch_keep_lambda(const Bufs& b, cudaStream_t st) { k_keep_lambda<<<grid(b.N), kThreads, 0, st>>>(b); }
 template <int V>
@@ -1919,7 +1951,8 @@ void launch_loop_next(const Bufs& b, cudaGraphConditionalHandle h, cudaStream_t 
   k_loop_next<<<1, 256, 0, st>>>(b, h);
 }
 void launch_compact(const Bufs& b, int k, int which, cudaStream_t st) {
-  k_compact<<<grid((b.N + kCompactSlots - 1) / kCompactSlots), kThreads, 0, st>>>(b, k, which);
+  k_compact<<<gridOf((b.N + kCompactSlots - 1) / kCompactSlots, kCompactThreads), kCompactThreads, 0, st>>>(b, k,
+                                                                                                       which);
 }
 void launch_solveA_list(const Bufs& b, int k, const float4* velIn, int flags, int variant, cudaStream_t st) {
   switch (variant) {

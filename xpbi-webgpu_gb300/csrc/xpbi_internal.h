@@ -18,7 +18,7 @@ constexpr int kSolveBVariants = 5;
 // dam breaches of 8k-120k solids and the 113k-solid snowball)
 constexpr uint64_t kFourLaneSolids = 24576;
 constexpr uint64_t kTwoLaneSolids = 49152;
-constexpr int kResidChunks = 512;      // per-scene partial sums of the residual
+constexpr int kResidBlocks = 256;      // at most this many partial sums of the residual per scene
 constexpr int kMaxResid = 129;         // residual slots per scene (iterations + 1)
 constexpr int kFeat = 16;              // network features per particle
 
@@ -143,7 +143,7 @@ struct Bufs {
   float* c0sq;          // [N] squared constraint value at the predicted velocities
   float* rc;            // [N] squared contact correction of the current iteration
   uint32_t* solidDisp;  // [2][S] float bits: largest dt |v| of a scene's solids entering iteration k (slot k & 1)
-  double* residPart;    // [S][kResidChunks][4] partial sums
+  double* residPart;    // [S][kResidBlocks][4] partial sums
   uint32_t* residTicket; // [S] blocks of the residual reduction done (0 between launches)
   double* resid;        // [S][kMaxResid] residual norm^2 per iteration (last slot: after the last)
   double* residC;       // [S][kMaxResid] contact residual norm^2, same slots
@@ -172,6 +172,7 @@ struct Bufs {
   int* err;             // [1] device error word
   unsigned long long* waitProbe;  // [1] a descriptor nothing publishes (xpbi_test_wait_expiry)
   uint32_t N, C, S;
+  uint32_t maxSceneN;   // particles of the largest scene
   uint32_t scanTiles;
 };
 
