@@ -599,14 +599,11 @@ cudaError_t enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Re
   R.mark(st, "fill");
   launch_reorder(b, sch.keepLam, st);
   R.mark(st, "reorder");
-  // the velocity-free sums are read by the one-lane constraint sweeps (and
-  // the features pass, which always has one lane)
-  launch_computeL(b, sch.lanes == 1 || sch.features, st);
+  // the velocity-free sums are read by the one-lane constraint sweeps; with
+  // features (the learned solve, or features logged) the same pass also
+  // stores iteration 0's constraint and the network's features
+  launch_computeL(b, sch.lanes == 1 || sch.features, sch.features, st);
   R.mark(st, "computeL");
-  if (sch.features) {
-    launch_features(b, b.velS[0], st);
-    R.mark(st, "features");
-  }
   if (sch.mode == 1) {
     mlp_forward(b.feat, b.N, b.netBlob, b.netOut, nullptr, s->netErr, st, true);
     R.mark(st, "network");
@@ -648,7 +645,7 @@ cudaError_t enqueueSubstep(xpbi_sim* s, const Schedule& sch, cudaStream_t st, Re
     if (sch.K - k0 >= 2) kLoop = k0;
   }
   for (int k = 0; k < kLoop; ++k) {
-    // iteration 0 after a features pass: that pass already evaluated the
+    // iteration 0 after computeL with features: it already evaluated the
     // constraint at these velocities, with one lane per slot (several lanes
     // sum in another order, so they evaluate it again)
     const int stored = k == 0 && sch.features && sch.lanes == 1 ? kStoredC : 0;
@@ -742,7 +739,6 @@ int kernelsPerSubstep(const Schedule& sch) {
     const bool list = sch.active && k >= 2;  // two compactions; before a PBF pass, the predicted positions
     n += 2 + (sch.pbf[k] ? 2 : 0) + (sch.reduce ? 1 : 0) + (list ? 2 + (sch.pbf[k] ? 1 : 0) : 0);
   }
-  if (sch.features) n += 1;
   if (sch.mode == 1) n += 2;
   if (sch.mode == 2) n += 1;
   if (sch.track) n += 3;
@@ -1374,7 +1370,7 @@ int xpbi_autotune(xpbi_sim* sim, int32_t iterations, int32_t has_water, int32_t 
     launch_scan(b, st);
     launch_scatter(b, st);
     launch_reorder(b, false, st);
-    launch_computeL(b, true, st);
+    launch_computeL(b, true, false, st);
     cudaMemsetAsync(b.done, 0, sizeof(int) * b.S, st);  // no scene counts as converged here
     cudaMemsetAsync(b.solidDisp, 0, sizeof(uint32_t) * 2 * b.S, st);
     // iteration 0 of each variant from lambda = 0, then solveB on its record

@@ -48,6 +48,13 @@ constexpr int kThreads = 128;
 #else
 #define XPBI_LB_COMPUTEL XPBI_LB_DEFAULT
 #endif
+// computeL with the stored constraint and features (the learned solve) at
+// 7 CTAs per SM (72 registers): 1.36 ms per 4M-particle substep against
+// 1.56 ms with the allocator's choice (5 CTAs).
+#ifndef XPBI_MINB_COMPUTEL_FEATURES
+#define XPBI_MINB_COMPUTEL_FEATURES 7
+#endif
+#define XPBI_LB_COMPUTEL_FEATURES __launch_bounds__(kThreads, XPBI_MINB_COMPUTEL_FEATURES)
 // solveA and solveB are compiled in several launch shapes — the block size
 // and the minimum resident CTAs per SM asked of the register allocator (0 =
 // its own choice) — and xpbi_autotune picks one per handle by timing them on
@@ -70,14 +77,6 @@ constexpr int kSolveBBlock[kSolveBVariants] = {128, 128, 128, 64, 256};
 #else
 #define XPBI_LB_UPDATE XPBI_LB_DEFAULT
 #endif
-// The features pass (the constraint sweep of solveA plus the stored
-// constraint and features) at 7 CTAs per SM (72 registers, ~100 bytes of
-// spills outside the neighbour loop): 0.48 ms per 4M-particle substep against
-// 0.60 ms with the allocator's 94 registers and 0.52 ms at 6 CTAs.
-#ifndef XPBI_MINB_FEATURES
-#define XPBI_MINB_FEATURES 7
-#endif
-#define XPBI_LB_FEATURES __launch_bounds__(kThreads, XPBI_MINB_FEATURES)
 
 struct Ctx {
   const SceneDev* __restrict__ scene;
@@ -279,20 +278,49 @@ __device__ __forceinline__ uint32_t recordCandidates(const SceneDev& S, const ui
   return cnt;
 }
 
+// A += V_b (v_b - v_i) g_b^T, the constraint sweep's velocity sum, with every
+// rounding explicit: solveA's sweep and computeL's (which stores iteration
+// 0's constraint for it) form the same bits whatever the compiler would
+// fuse around them.
+__device__ __forceinline__ void addVelSum(M3& A, const float4& vb, V3 vi, V3 g) {
+  const float dx = __fmul_rn(__fsub_rn(vb.x, vi.x), vb.w);
+  const float dy = __fmul_rn(__fsub_rn(vb.y, vi.y), vb.w);
+  const float dz = __fmul_rn(__fsub_rn(vb.z, vi.z), vb.w);
+  const float gc[3] = {g.x, g.y, g.z};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    A.c[c].x = __fmaf_rn(dx, gc[c], A.c[c].x);
+    A.c[c].y = __fmaf_rn(dy, gc[c], A.c[c].y);
+    A.c[c].z = __fmaf_rn(dz, gc[c], A.c[c].z);
+  }
+}
+
 // ---------------------------------------------------------------- computeL
 // L of slot i (simkernels.js:198-220) over its recorded neighbours: the
 // SVD pseudo-inverse of sum V_b (grad W_b) (x_b - x_i)^T. For a solid
 // (kSolid) the same sweep also forms the sums of the constraint passes that
 // no velocity enters — s = sum V_b g_b, P = sum (V_b^2 / m_b) g_b g_b^T and
 // the solid neighbour count, over the solid neighbours in list order — and
-// stores them in sgP for every iteration of the substep.
-template <bool kSolid>
-__device__ __forceinline__ void bonetLok(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi) {
+// stores them in sgP for every iteration of the substep. With kVel (a solid,
+// at the velocities iteration 0 starts from) the sweep also forms that
+// iteration's velocity sum Av = sum V_b (v_b - v_i) g_b^T over the solid
+// neighbours in list order — the constraint sweep's own expression — and
+// hands the sums and L to the caller.
+struct SweepSums {
+  M3 Av, L;
+  V3 sg;
+  float p00, p11, p22, p01, p02, p12, cnt;
+};
+template <bool kSolid, bool kVel = false>
+__device__ __forceinline__ void bonetLok(const Bufs& b, const Ctx& cx, uint32_t i, V3 xi, SweepSums* out = nullptr) {
+  static_assert(kSolid || !kVel, "the velocity sum is a solid's");
   const SceneDev& S = *cx.scene;
   const float4* __restrict__ posS = b.posS;
-  const float4* __restrict__ velIn = b.velS[0];  // only V^n (.w) is read, which no pass changes
-  M3 A = mzero();
+  const float4* __restrict__ velIn = b.velS[0];  // V^n (.w), which no pass changes; with kVel also v
+  M3 A = mzero(), Av = mzero();
   V3 sg = splat(0.f);
+  V3 vi = splat(0.f);
+  if constexpr (kVel) vi = xyz(velIn[i]);
   float p00 = 0.f, p11 = 0.f, p22 = 0.f, p01 = 0.f, p02 = 0.f, p12 = 0.f, cnt = 0.f;
   forNbrs(b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
           [&](uint32_t, bool water, const PV& d) {
@@ -309,6 +337,7 @@ __device__ __forceinline__ void bonetLok(const Bufs& b, const Ctx& cx, uint32_t 
               A.c[c].z = __fmaf_rn(__fmul_rn(g.z, r[c]), Vb0, A.c[c].z);
             }
             if (kSolid && !water) {
+              if constexpr (kVel) addVelSum(Av, d.v, vi, g);
               const float Vb = d.v.w;
               sg = sg + g * Vb;
               const float c = Vb * Vb / cx.mats[matOfW(d.p.w)].mass;
@@ -335,35 +364,10 @@ __device__ __forceinline__ void bonetLok(const Bufs& b, const Ctx& cx, uint32_t 
   if (fabsf(s.sig.x) > tol) inv.x = __frcp_rn(s.sig.x);
   if (fabsf(s.sig.y) > tol) inv.y = __frcp_rn(s.sig.y);
   if (fabsf(s.sig.z) > tol) inv.z = __frcp_rn(s.sig.z);
-  storeM(b.L, b.N, i, diagMul(s.V, inv, s.U));
+  const M3 L = diagMul(s.V, inv, s.U);
+  storeM(b.L, b.N, i, L);
+  if constexpr (kVel) *out = SweepSums{Av, L, sg, p00, p11, p22, p01, p02, p12, cnt};
 }
-// Bonet-Lok correction with SVD pseudo-inverse (simkernels.js:189-221); its
-// candidate walk records the substep's neighbour list.
-template <bool kSums>
-__global__ void XPBI_LB_COMPUTEL k_computeL(Bufs b) {
-  // blocks run last to first: the pass starts where the reorder ended, on
-  // slots whose data is still in L2
-  const uint32_t i = (gridDim.x - 1u - blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= b.N) return;
-  const Ctx cx = ctxOf(b, i);
-  const SceneDev& S = *cx.scene;
-  const float4* __restrict__ posS = b.posS;
-  const float4* __restrict__ velIn = b.velS[0];
-  const V3 xi = xyz(posS[i]);
-  const float s2 = S.support2;
-  const uint32_t cnt = recordCandidates(S, b.cellStart, xi, i, listOf(b.nbr, i), [&](uint32_t j, uint32_t& e) {
-    const float4 p = ldg(posS + j);
-    const V3 d = xi - xyz(p);
-    e = j | (__float_as_uint(p.w) & kWaterBit);  // the water flag is the sign bit of pos.w
-    return dot(d, d) < s2;
-  });
-  b.nbrCount[i] = cnt <= kNbrCap ? cnt : kNbrOverflow;
-  // no pass of the substep reads a water particle's correction (every
-  // velocity gradient is a solid's): k_computeL_water forms it when the state
-  // is read
-  if (!waterW(posS[i].w)) bonetLok<kSums>(b, cx, i, xi);
-}
-
 // The water particles' L of the last substep, from the same positions,
 // neighbour lists and V^n as k_computeL would have used.
 __global__ void XPBI_LB_COMPUTEL k_computeL_water(Bufs b) {
@@ -440,6 +444,14 @@ struct Constraint {
   float nNbr;     // solid neighbours in the sweep
 };
 
+// (Compiled once, not inlined: solveA and computeL with features run the
+// same instructions, so iteration 0's stored constraint is bit for bit the
+// one solveA would evaluate; inlined, the compiler fuses multiplies and adds
+// differently in each kernel.)
+__device__ __noinline__ Constraint constraintFromSums(const SceneDev& S, const M3& A, V3 sg, float p00, float p11,
+                                                     float p22, float p01, float p02, float p12, float cnt,
+                                                     const M3& Li, const M3& Fn, const MatDev& m, float st);
+
 template <int NL = 1>
 __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& cx, uint32_t i, float4 pi,
                                                      const float4* __restrict__ velIn, const MatDev& m, float st,
@@ -463,9 +475,7 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
         b, cx, i, xi, [&](uint32_t j) { return PV{ldg(posS + j), ldg(velIn + j)}; },
         [&](uint32_t, bool water, const PV& d) {
           if (water) return;
-          const V3 g = gradWFast(S, xi - xyz(d.p));
-          const V3 dv = (xyz(d.v) - vi) * d.v.w;
-          A = madd(A, M3{{dv * g.x, dv * g.y, dv * g.z}});
+          addVelSum(A, d.v, vi, gradWFast(S, xi - xyz(d.p)));
         },
         SolidOnly{});
     const float4* __restrict__ R = b.sgP + i;
@@ -486,8 +496,7 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
           if (water) return;
           const V3 g = gradWFast(S, xi - xyz(d.p));
           const float Vb = d.v.w;
-          const V3 dv = (xyz(d.v) - vi) * Vb;
-          A = madd(A, M3{{dv * g.x, dv * g.y, dv * g.z}});
+          addVelSum(A, d.v, vi, g);
           sg = sg + g * Vb;
           const float c = Vb * Vb / cx.mats[matOfW(d.p.w)].mass;
           const V3 cg = g * c;
@@ -514,7 +523,16 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
     cnt = laneSum<NL>(cnt);
     if (lane != 0) return Constraint{};  // lane 0 finishes the slot
   }
-  const M3 Li = loadM(b.L, b.N, i);
+  return constraintFromSums(S, A, sg, p00, p11, p22, p01, p02, p12, cnt, loadM(b.L, b.N, i), loadM(b.FS, b.N, i), m,
+                            st);
+}
+
+// The per-particle part of the constraint from the sweep's sums (A = sum dv
+// g^T, s = sum V g, P = sum (V^2/m) g g^T over the solid neighbours in list
+// order, their count), the slot's correction L and its F.
+__device__ __noinline__ Constraint constraintFromSums(const SceneDev& S, const M3& A, V3 sg, float p00, float p11,
+                                                     float p22, float p01, float p02, float p12, float cnt,
+                                                     const M3& Li, const M3& Fn, const MatDev& m, float st) {
   const M3 LiT = transpose(Li);
   const M3 G = mul(A, LiT);
   const V3 sv = mul(Li, sg);
@@ -523,7 +541,6 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
   const float q01 = Qm.c[1].x, q02 = Qm.c[2].x, q12 = Qm.c[2].y;
   Constraint out;
   out.nNbr = cnt;
-  const M3 Fn = loadM(b.FS, b.N, i);
   const M3 Ftr = mul(madd(mident(), mscale(G, S.dt)), Fn);
   const SVD sd = svd3Fast(Ftr);
   out.logSigTr = vlog(safeSig(sd.sig));
@@ -554,7 +571,7 @@ __device__ __forceinline__ Constraint evalConstraint(const Bufs& b, const Ctx& c
 }
 
 // The iteration-0 constraint of slot i in four float4 planes (plane q of
-// slot i at cons0[q N + i]): the features pass evaluates it at the very
+// slot i at cons0[q N + i]): computeL with features evaluates it at the very
 // velocities iteration 0 starts from, so iteration 0 can read it instead of
 // sweeping the neighbours again.
 __device__ __forceinline__ void storeConstraint(const Bufs& b, uint32_t i, const Constraint& c) {
@@ -701,9 +718,9 @@ __device__ __forceinline__ int iterK(const Bufs& b, int k) {
 //   replaced by the plain start lambda0 = 0 (the plain solve stays the
 //   fallback). With lambda0 = 0 both updates are the reference's.
 // flags & kMeasureOnly: residual only (the pass after the last iteration).
-// flags & kStoredC (iteration 0, after the features pass, one lane per
-//   slot): the constraint is the one the features pass evaluated at the
-//   same velocities; k_solveA_stored applies it without a neighbour sweep.
+// flags & kStoredC (iteration 0, after computeL with features, one lane per
+//   slot): the constraint is the one computeL evaluated at the same
+//   velocities; k_solveA_stored applies it without a neighbour sweep.
 // G lanes per slot (G = 4 for small scenes): the lanes split the neighbour
 // sweep, lane 0 finishes the slot.
 //
@@ -889,7 +906,7 @@ __global__ void __launch_bounds__(kBlock, kMinB) k_solveA_list(Bufs b, int k, co
   (void)flags;
 }
 
-// Iteration 0 after the features pass: the constraint that pass stored at
+// Iteration 0 after computeL with features: the constraint it stored at
 // these velocities (bit-identical to evaluating it), no neighbour sweep — a
 // register-light launch at full occupancy in place of the sweep kernel.
 template <bool kTrack>
@@ -922,39 +939,85 @@ __global__ void __launch_bounds__(kThreads) k_solveA_stored(Bufs b, const float4
 //   7    solid neighbours / 32
 //   8-14 material kind one-hot
 //   15   log10(mu) - 4.5
-__global__ void XPBI_LB_FEATURES k_features(Bufs b, const float4* __restrict__ velIn) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= b.N) return;
-  const Ctx cx = ctxOf(b, i);
-  const SceneDev& S = *cx.scene;
-  const float4 pi = b.posS[i];
-  float f[kFeat];
+__device__ __forceinline__ void fillFeatures(float (&f)[kFeat], const SceneDev& S, const Constraint& c, float lamPrev,
+                                             uint32_t kind, const MatDev& m) {
+  const float aT = S.alphaT;
+  f[0] = c.logSigTr.x;
+  f[1] = c.logSigTr.y;
+  f[2] = c.logSigTr.z;
+  f[3] = c.C;
+  f[4] = aT * lamPrev;
+  f[5] = -c.C * aT / (c.denom + aT);
+  f[6] = log10f(1.f + c.denom / aT);
+  f[7] = c.nNbr * (1.f / 32.f);
 #pragma unroll
-  for (int q = 0; q < kFeat; ++q) f[q] = 0.f;
-  if (!waterW(pi.w) && S.iterations > 0) {
-    const uint32_t mi = matOfW(pi.w);
-    const float st = b.stateS[i];
-    const MatDev m = hardenedMat(cx.mats[mi], st);
-    const Constraint c = evalConstraint(b, cx, i, pi, velIn, m, st);
-    storeConstraint(b, i, c);
-    const float aT = S.alphaT;
-    f[0] = c.logSigTr.x;
-    f[1] = c.logSigTr.y;
-    f[2] = c.logSigTr.z;
-    f[3] = c.C;
-    f[4] = aT * b.lamPrev[i];
-    f[5] = -c.C * aT / (c.denom + aT);
-    f[6] = log10f(1.f + c.denom / aT);
-    f[7] = c.nNbr * (1.f / 32.f);
-    const uint32_t kind = cx.mats[mi].kind;
-#pragma unroll
-    for (uint32_t q = 0; q < 7u; ++q) f[8 + q] = kind == q ? 1.f : 0.f;  // constant indices: f stays in registers
-    f[15] = log10f(fmaxf(m.mu, 1e-6f)) - 4.5f;
-  }
+  for (uint32_t q = 0; q < 7u; ++q) f[8 + q] = kind == q ? 1.f : 0.f;  // constant indices: f stays in registers
+  f[15] = log10f(fmaxf(m.mu, 1e-6f)) - 4.5f;
+}
+__device__ __forceinline__ void storeFeatures(const Bufs& b, uint32_t i, const float (&f)[kFeat]) {
   float4* out = reinterpret_cast<float4*>(b.feat + (size_t)i * kFeat);
 #pragma unroll
   for (int q = 0; q < kFeat / 4; ++q) out[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
 }
+
+// Bonet-Lok correction with SVD pseudo-inverse (simkernels.js:189-221); its
+// candidate walk records the substep's neighbour list. kFeatures (the
+// learned solve, or features logged): the same sweep forms iteration 0's
+// velocity sum, so iteration 0's constraint (the arithmetic solveA's sweep
+// would do, from the same sums in the same order) is stored for
+// k_solveA_stored here, with the network's features (fillFeatures; zeros
+// for water and for scenes without iterations), without a second sweep of
+// every solid's neighbours.
+template <bool kSums, bool kFeatures>
+__device__ __forceinline__ void computeL(const Bufs& b) {
+  static_assert(kSums || !kFeatures, "the features need the sums");
+  // blocks run last to first: the pass starts where the reorder ended, on
+  // slots whose data is still in L2
+  const uint32_t i = (gridDim.x - 1u - blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= b.N) return;
+  const Ctx cx = ctxOf(b, i);
+  const SceneDev& S = *cx.scene;
+  const float4* __restrict__ posS = b.posS;
+  const float4 pi = posS[i];
+  const V3 xi = xyz(pi);
+  const float s2 = S.support2;
+  const uint32_t cnt = recordCandidates(S, b.cellStart, xi, i, listOf(b.nbr, i), [&](uint32_t j, uint32_t& e) {
+    const float4 p = ldg(posS + j);
+    const V3 d = xi - xyz(p);
+    e = j | (__float_as_uint(p.w) & kWaterBit);  // the water flag is the sign bit of pos.w
+    return dot(d, d) < s2;
+  });
+  b.nbrCount[i] = cnt <= kNbrCap ? cnt : kNbrOverflow;
+  // no pass of the substep reads a water particle's correction (every
+  // velocity gradient is a solid's): k_computeL_water forms it when the state
+  // is read
+  if constexpr (kFeatures) {
+    float f[kFeat];
+#pragma unroll
+    for (int q = 0; q < kFeat; ++q) f[q] = 0.f;
+    if (!waterW(pi.w)) {
+      SweepSums w;
+      bonetLok<true, true>(b, cx, i, xi, &w);
+      if (S.iterations > 0) {
+        const uint32_t mi = matOfW(pi.w);
+        const float st = b.stateS[i];
+        const MatDev m = hardenedMat(cx.mats[mi], st);
+        const Constraint c = constraintFromSums(S, w.Av, w.sg, w.p00, w.p11, w.p22, w.p01, w.p02, w.p12, w.cnt, w.L,
+                                                loadM(b.FS, b.N, i), m, st);
+        storeConstraint(b, i, c);
+        fillFeatures(f, S, c, b.lamPrev[i], cx.mats[mi].kind, m);
+      }
+    }
+    storeFeatures(b, i, f);
+  } else {
+    if (!waterW(pi.w)) bonetLok<kSums>(b, cx, i, xi);
+  }
+}
+template <bool kSums>
+__global__ void XPBI_LB_COMPUTEL k_computeL(Bufs b) {
+  computeL<kSums, false>(b);
+}
+__global__ void XPBI_LB_COMPUTEL_FEATURES k_computeL_features(Bufs b) { computeL<true, true>(b); }
 
 // lambda_warm = previous multiplier + network output / alphaT (the network
 // predicts alphaT times the increment over the previous substep's multiplier)
@@ -1830,8 +1893,10 @@ inline unsigned gridOf(uint32_t n, int block) { return (unsigned)((n + (uint32_t
 
 }  // namespace
 
-void launch_computeL(const Bufs& b, bool sums, cudaStream_t st) {
-  if (sums)
+void launch_computeL(const Bufs& b, bool sums, bool features, cudaStream_t st) {
+  if (features)
+    k_computeL_features<<<grid(b.N), kThreads, 0, st>>>(b);
+  else if (sums)
     k_computeL<true><<<grid(b.N), kThreads, 0, st>>>(b);
   else
     k_computeL<false><<<grid(b.N), kThreads, 0, st>>>(b);
@@ -1847,7 +1912,7 @@ void solveAVariant(const Bufs& b, int k, const float4* velIn, int flags, cudaStr
         b, k, velIn, flags);
 }
 void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, int variant, int lanes, cudaStream_t st) {
-  if (flags & kStoredC) {  // iteration 0 after the features pass (one lane per slot)
+  if (flags & kStoredC) {  // iteration 0 after computeL with features (one lane per slot)
     if (flags & kTrackResid)
       k_solveA_stored<true><<<grid(b.N), kThreads, 0, st>>>(b, velIn, flags);
     else
@@ -1878,9 +1943,6 @@ void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, int var
     case 5: solveAVariant<5>(b, k, velIn, flags, st); break;
     default: solveAVariant<0>(b, k, velIn, flags, st); break;
   }
-}
-void launch_features(const Bufs& b, const float4* velIn, cudaStream_t st) {
-  k_features<<<grid(b.N), kThreads, 0, st>>>(b, velIn);
 }
 void launch_warm_from_net(const Bufs& b, cudaStream_t st) { k_warm_from_net<<<grid(b.N), kThreads, 0, st>>>(b); }
 void launch_warm_from_prev(const Bufs& b, cudaStream_t st) { k_warm_from_prev<<<grid(b.N), kThreads, 0, st>>>(b); }

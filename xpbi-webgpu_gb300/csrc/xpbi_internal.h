@@ -26,7 +26,7 @@ constexpr int kFeat = 16;              // network features per particle
 constexpr int kTrackResid = 1;         // write per-particle residuals
 constexpr int kWarm = 2;               // iteration 0 starts from lamWarm
 constexpr int kMeasureOnly = 4;        // residual only: no multiplier / impulse update
-constexpr int kStoredC = 8;            // iteration 0 reads the constraint the features pass stored
+constexpr int kStoredC = 8;            // iteration 0 reads the constraint computeL stored (features)
 // active set (solveA / solveB / pbfB flags)
 constexpr int kMarkMoved = 16;         // a slot whose velocity changed marks itself (and, if solid, its solid
                                        // neighbours) as changed for the next iteration
@@ -137,7 +137,7 @@ struct Bufs {
   float* lamPrev;       // [N] the same, carried into this substep's sorted order
   float* lamWarm;       // [N] warm-start multiplier for iteration 0 (sorted)
   float* feat;          // [N][16] network features at iteration 0 (sorted)
-  float4* cons0;        // [4][N] the features pass's iteration-0 constraint: C, denom, cdot, sgrad, GL
+  float4* cons0;        // [4][N] iteration 0's constraint stored by computeL: C, denom, cdot, sgrad, GL
   float* netOut;        // [N] network output
   float* rr;            // [N] squared constraint residual of the current iteration
   float* c0sq;          // [N] squared constraint value at the predicted velocities
@@ -186,12 +186,12 @@ void launch_warm_from_prev(const Bufs& b, cudaStream_t st);
 uint32_t scan_tiles(uint32_t cells);
 
 // ---- launchers (solve.cu) ----
-// sums: also form the solids' velocity-free constraint sums (sgP)
-void launch_computeL(const Bufs& b, bool sums, cudaStream_t st);
+// sums: also form the solids' velocity-free constraint sums (sgP);
+// features: also iteration 0's constraint (cons0) and the network features
+void launch_computeL(const Bufs& b, bool sums, bool features, cudaStream_t st);
 // the water particles' L of the last substep (computeL forms the solids' only)
 void launch_computeL_water(const Bufs& b, cudaStream_t st);
 void launch_solveA(const Bufs& b, int k, const float4* velIn, int flags, int variant, int lanes, cudaStream_t st);
-void launch_features(const Bufs& b, const float4* velIn, cudaStream_t st);
 void launch_warm_from_net(const Bufs& b, cudaStream_t st);
 void launch_resid_reduce(const Bufs& b, int k, bool warm, cudaStream_t st);
 void launch_keep_lambda(const Bufs& b, cudaStream_t st);
