@@ -57,8 +57,8 @@ def test_tracking_does_not_change_the_solve(xp, built_lib):
 @pytest.mark.parametrize("lanes,track", [(0, False), (1, False), (1, True)])
 def test_zero_network_is_the_previous_multiplier_start(xp, built_lib, lanes, track):
     """The network predicts an increment over the previous multiplier. With
-    one lane per slot the network mode's iteration 0 reads the constraint its
-    features pass evaluated (k_solveA_stored, with or without residual
+    one lane per slot the network mode's iteration 0 reads the constraint
+    computeL evaluated with the features (k_solveA_stored, with or without residual
     tracking), the previous-multiplier mode evaluates it in solveA: both must
     give the same bytes."""
     sc = xp.scenes.dam_breach()
