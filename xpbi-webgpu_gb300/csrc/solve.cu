@@ -58,12 +58,14 @@ constexpr int kThreads = 128;
 // solveA and solveB are compiled in several launch shapes — the block size
 // and the minimum resident CTAs per SM asked of the register allocator (0 =
 // its own choice) — and xpbi_autotune picks one per handle by timing them on
-// its data. Entry 0 is the default: for solveA 7 CTAs of 128 per SM (72
-// registers, a few spills outside the neighbour loop) measured 15% faster
-// than the allocator's own choice on the 4M-particle dam-breach mix; for
+// its data. Entry 0 is the default: for solveA 8 CTAs of 128 per SM (64
+// registers; the constraint's per-particle tail is a separately compiled
+// function) — 0.396 ms per launch on the 4M-particle dam-breach mix against
+// 0.417 at 7 CTAs, 0.421 at 9, 0.438 at 10 and 0.58 at 5, and the best or
+// within 1% on the 256-scene batch, the snowball and the sand column; for
 // solveB the allocator's choice (80 registers) beat every cap. The 64- and
 // 256-thread shapes keep an entry's occupancy with other block sizes.
-constexpr int kSolveAMinB[kSolveAVariants] = {7, 6, 5, 8, 14, 4};
+constexpr int kSolveAMinB[kSolveAVariants] = {8, 6, 5, 7, 14, 4};
 constexpr int kSolveABlock[kSolveAVariants] = {128, 128, 128, 128, 64, 256};
 constexpr int kSolveBMinB[kSolveBVariants] = {0, 7, 5, 0, 0};
 constexpr int kSolveBBlock[kSolveBVariants] = {128, 128, 128, 64, 256};
