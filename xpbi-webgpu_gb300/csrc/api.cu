@@ -279,6 +279,15 @@ struct xpbi_sim {
   std::vector<SceneDev> sdev;
   std::vector<MatDev> mdev;
   std::vector<uint32_t> matWordsHost;
+  // page-locked staging of the uniforms, a ring of kUploadRing slots each
+  // reused once its copy completed: a copy from pageable memory would first
+  // wait for the stream's earlier work, so a frame's writeParams + step
+  // could not be queued while the previous substep runs
+  static constexpr int kUploadRing = 3;
+  uint8_t* upHost[kUploadRing] = {};
+  cudaEvent_t upDone[kUploadRing] = {};
+  size_t upCap = 0;
+  int upNext = 0;
   uint32_t* matWords = nullptr;  // packed reference material table [S*128] (renderer binding)
   bool dirty = true;
   bool fresh = true;
@@ -345,6 +354,11 @@ void destroyAll(xpbi_sim* s) {
   if (s->loop) cudaStreamDestroy(s->loop);
   if (s->evWork) cudaEventDestroy(s->evWork);
   if (s->evCopy) cudaEventDestroy(s->evCopy);
+  for (int j = 0; j < xpbi_sim::kUploadRing; ++j) {
+    if (s->upDone[j]) cudaEventSynchronize(s->upDone[j]);
+    if (s->upHost[j]) cudaFreeHost(s->upHost[j]);
+    if (s->upDone[j]) cudaEventDestroy(s->upDone[j]);
+  }
 }
 
 // Work outside the substep that rewrites the positions waits for the
@@ -374,11 +388,33 @@ int upload(xpbi_sim* s) {
     for (uint32_t m = 0; m < s->sc[i].nMats; ++m)
       packMaterial(s->sc[i].mats[m], s->sc[i].V0, &s->matWordsHost[((size_t)i * kMaxMats + m) * XPBI_MATERIAL_WORDS]);
   }
-  XPBI_CK(cudaMemcpyAsync(s->b.scenes, s->sdev.data(), sizeof(SceneDev) * S, cudaMemcpyHostToDevice, s->stream));
-  XPBI_CK(cudaMemcpyAsync(s->b.mats, s->mdev.data(), sizeof(MatDev) * s->mdev.size(), cudaMemcpyHostToDevice,
-                          s->stream));
-  XPBI_CK(cudaMemcpyAsync(s->matWords, s->matWordsHost.data(), 4 * s->matWordsHost.size(), cudaMemcpyHostToDevice,
-                          s->stream));
+  const size_t bS = sizeof(SceneDev) * S, bM = sizeof(MatDev) * s->mdev.size(), bW = 4 * s->matWordsHost.size();
+  const size_t oM = (bS + 255) & ~size_t(255), oW = (oM + bM + 255) & ~size_t(255), need = oW + bW;
+  if (need > s->upCap) {  // (re)allocate the ring: wait for the copies that read the old one
+    for (int j = 0; j < xpbi_sim::kUploadRing; ++j) {
+      if (s->upDone[j]) XPBI_CK(cudaEventSynchronize(s->upDone[j]));
+      if (s->upHost[j]) cudaFreeHost(s->upHost[j]);
+      s->upHost[j] = nullptr;
+    }
+    s->upCap = 0;
+    for (int j = 0; j < xpbi_sim::kUploadRing; ++j) {
+      if (cudaMallocHost(reinterpret_cast<void**>(&s->upHost[j]), need) != cudaSuccess)
+        return fail(XPBI_ERR_OOM, "page-locked staging of the uniforms");
+      if (!s->upDone[j]) XPBI_CK(cudaEventCreateWithFlags(&s->upDone[j], cudaEventDisableTiming));
+    }
+    s->upCap = need;
+  }
+  const int j = s->upNext;
+  s->upNext = (j + 1) % xpbi_sim::kUploadRing;
+  XPBI_CK(cudaEventSynchronize(s->upDone[j]));  // this slot's last copy, kUploadRing uploads ago
+  uint8_t* h = s->upHost[j];
+  std::memcpy(h, s->sdev.data(), bS);
+  std::memcpy(h + oM, s->mdev.data(), bM);
+  std::memcpy(h + oW, s->matWordsHost.data(), bW);
+  XPBI_CK(cudaMemcpyAsync(s->b.scenes, h, bS, cudaMemcpyHostToDevice, s->stream));
+  XPBI_CK(cudaMemcpyAsync(s->b.mats, h + oM, bM, cudaMemcpyHostToDevice, s->stream));
+  XPBI_CK(cudaMemcpyAsync(s->matWords, h + oW, bW, cudaMemcpyHostToDevice, s->stream));
+  XPBI_CK(cudaEventRecord(s->upDone[j], s->stream));
   s->dirty = false;
   return XPBI_OK;
 }
