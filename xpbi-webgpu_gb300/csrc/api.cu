@@ -343,6 +343,11 @@ int alloc(xpbi_sim* s, T** p, size_t count) {
   } while (0)
 
 void destroyAll(xpbi_sim* s) {
+  for (int j = 0; j < xpbi_sim::kUploadRing; ++j) {  // no copy may still read a staging slot
+    if (s->upDone[j]) cudaEventSynchronize(s->upDone[j]);
+    if (s->upHost[j]) cudaFreeHost(s->upHost[j]);
+    if (s->upDone[j]) cudaEventDestroy(s->upDone[j]);
+  }
   if (s->gexec) cudaGraphExecDestroy(s->gexec);
   if (s->graph) cudaGraphDestroy(s->graph);
   for (void* p : s->allocs) cudaFree(p);
@@ -354,11 +359,6 @@ void destroyAll(xpbi_sim* s) {
   if (s->loop) cudaStreamDestroy(s->loop);
   if (s->evWork) cudaEventDestroy(s->evWork);
   if (s->evCopy) cudaEventDestroy(s->evCopy);
-  for (int j = 0; j < xpbi_sim::kUploadRing; ++j) {
-    if (s->upDone[j]) cudaEventSynchronize(s->upDone[j]);
-    if (s->upHost[j]) cudaFreeHost(s->upHost[j]);
-    if (s->upDone[j]) cudaEventDestroy(s->upDone[j]);
-  }
 }
 
 // Work outside the substep that rewrites the positions waits for the
