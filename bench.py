@@ -592,12 +592,25 @@ def run_profile_region(args):
     warm-up substeps from its graph, then two substeps inside
     cudaProfilerStart/Stop, replayed from the graph (`graph`; ncu times it
     whole) or enqueued launch by launch (`eager`; the same kernels, with the
-    iterations past the stop enqueued as launches that find nothing to do)."""
+    iterations past the stop enqueued as launches that find nothing to do).
+    `plain`: the plain solve (autotuned as the bench line's) after the same
+    preroll, one substep enqueued launch by launch inside the region."""
     import torch
     torch.cuda.set_device(0)
     xp, scenes, _ = workload(args.workload, 0, 1)
     stream = torch.cuda.Stream()
     sim, has_water = make_sim(xp, scenes, stream, args.preroll)
+    if args.profile_region == "plain":
+        sim.set_solver(0, 0.0, False, False)
+        tuned = sim.autotune(-1, has_water, repeats=3)
+        sim.step(3, -1, has_water)
+        sim.synchronize()
+        torch.cuda.profiler.start()
+        sim.encode_substep(-1, has_water)
+        sim.synchronize()
+        torch.cuda.profiler.stop()
+        print(json.dumps({"profile_region": "plain", "workload": args.workload, "variants": tuned}))
+        return
     sim.set_solver(0, 0.0, True, True)
     rel, relc, _ = residual_stats(sim, has_water, len(scenes), args.residual_substeps)
     tau, tau_c = float(np.median(rel)), float(np.median(relc))
@@ -644,8 +657,9 @@ def main():
     ap.add_argument("--max-iterations", type=int, default=30,
                     help="iteration cap of the early-stopped solves (they stop once both residuals reach the plain "
                          "solve's; the plain solve runs its fixed 15)")
-    ap.add_argument("--profile-region", choices=["graph", "eager"], default=None,
-                    help="set up the learned solve and run two substeps between cudaProfilerStart/Stop (for ncu "
+    ap.add_argument("--profile-region", choices=["graph", "eager", "plain"], default=None,
+                    help="set up the learned solve (graph, eager: two substeps) or the plain one (plain: one substep) "
+                         "and run it between cudaProfilerStart/Stop (for ncu "
                          "--profile-from-start off); prints no bench line")
     ap.add_argument("--no-other-configs", action="store_true",
                     help="skip the plain solve of the sand column, snowball and 256-scene batch configs")
