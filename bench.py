@@ -52,9 +52,11 @@ ALGO_BYTES = {"solveA": (196, 16), "solveB": (128, 48), "pbfA": (36, 36), "pbfB"
 
 # DRAM bytes per particle per launch (dram__bytes_read.sum +
 # dram__bytes_write.sum over particles) from an ncu --set full capture of the
-# current kernels on the 1M-particle dam breach; the traffic of a launch grows
-# with the particle count, so the bench scales it by the workload's.
-NCU_TRAFFIC_PER_PARTICLE = {"solveB": 127.8, "solveA": 153.7, "pbfA": 105.6, "computeL": 229.5}
+# current kernels on the 1M-particle dam breach 100 plain substeps in (the
+# bench's loaded state; profiles/stencil_kernels_full_dam_breach_1M.md); the
+# traffic of a launch grows with the particle count, so the bench scales it
+# by the workload's.
+NCU_TRAFFIC_PER_PARTICLE = {"solveB": 145.6, "solveA": 213.2, "pbfA": 107.2, "computeL": 169.7}
 
 
 def workload(name: str, rank: int = 0, world: int = 1):
@@ -536,7 +538,7 @@ def run_xpbi(args, rank: int, world: int):
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_src,
                 "traffic": None if tpp is None else tpp * n_rank,
-                "traffic_source": "ncu capture of the 1M-particle dam breach scaled by particle count",
+                "traffic_source": "ncu capture of the 1M-particle dam breach (100 substeps in) scaled by particle count",
                 "algo_bytes_per_launch": algo, "solid_particles": n_solid, "water_particles": n_water,
                 "share": sum(per[dom]) / total_ms,
                 "kernel_ms": {k: round(statistics.mean(v), 4) for k, v in per.items()}}
